@@ -1,0 +1,114 @@
+/*
+ * powerfit_gb300 — C ABI of the GB300 (sm_103a) exhaustive 6D local
+ * cross-correlation search.
+ *
+ * Every entry point takes plain pointers and sizes (no framework types),
+ * returns 0 on success and a negative PF_E* code on failure; a failing call
+ * never aborts the process.  The message of the last failure is available
+ * from pf_last_error() (per context) or pf_global_error() (calls without a
+ * context).  Arrays are C-order (z, y, x), host memory unless the name says
+ * otherwise.
+ *
+ * Reference interfaces replaced (file:line in haddocking/powerfit v3.0.2):
+ *   correlator object  src/powerfit_em/powerfitter.py:166-393 (BaseCorrelator,
+ *                      CPUCorrelator) and :396-555 (GPUCorrelator)
+ *   native helpers     src/powerfit_em/_extensions.c:7-196 (rotate_grid3d),
+ *                      src/powerfit_em/_powerfit.pyx:45-72 (conj_multiply,
+ *                      calc_lcc)
+ *   shard merge        src/powerfit_em/powerfitter.py:146-163 (_combine)
+ */
+#ifndef POWERFIT_GB300_H
+#define POWERFIT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PF_OK 0
+#define PF_E_ARG (-1)       /* bad argument (shape, size, pointer, order of calls) */
+#define PF_E_CUDA (-2)      /* CUDA runtime error */
+#define PF_E_NOMEM (-3)     /* device allocation failed */
+#define PF_E_STATE (-4)     /* target / template / rotations not set */
+#define PF_E_SHAPE (-5)     /* grid size not supported (prime factor > 7, plane too large) */
+
+/* pf_scan flags */
+#define PF_FLAG_FP64_NORM 1   /* local variance and LCC in float64 (default: float-float) */
+#define PF_FLAG_NO_PRUNE 2    /* do not skip rotated rows known to be zero */
+#define PF_FLAG_ACCUMULATE 4  /* keep the running best of earlier scans (do not reset) */
+
+typedef struct pf_ctx pf_ctx;
+
+/* --- correlator context: one per (grid shape, device); replaces the
+ *     constructor of CPUCorrelator/GPUCorrelator (powerfitter.py:262-277,
+ *     :399-424) ------------------------------------------------------------ */
+pf_ctx *pf_create(int nz, int ny, int nx, int device, int *status);
+int pf_destroy(pf_ctx *ctx);
+int pf_last_error(const pf_ctx *ctx, char *buf, size_t len);
+int pf_global_error(char *buf, size_t len);
+
+/* Target, already normalised by its maximum and Laplace-filtered if the
+ * search uses the Laplace pre-filter (powerfitter.py:268-277), and the lcc
+ * mask (target > 0.05 max of the unfiltered target, powerfitter.py:178-180).
+ * Computes FT(target) and FT(target^2) on the device. */
+int pf_set_target(pf_ctx *ctx, const double *target, const uint8_t *lcc_mask);
+
+/* Template after the mask setter's preprocessing (Laplace, mask, normalise,
+ * mask again: powerfitter.py:190-220), the mask, the number of mask voxels
+ * (norm_factor, :199) and the rotation radius rmax (min(shape)//2, :176). */
+int pf_set_template_mask(pf_ctx *ctx, const double *tmpl, const double *mask, double norm_factor, int rmax);
+
+/* One-shot scan of nrot row-major 3x3 rotation matrices (powerfitter.py:
+ * 317-333): per voxel the best LCC (strict >, initial 0, lowest index wins
+ * ties) and the index of the rotation that gave it, plus rot_offset.
+ * out_lcc/out_rot: nz*ny*nx float32 / int32 (GPUCorrelator.lcc/.rot types). */
+int pf_scan(pf_ctx *ctx, const double *rotmats, int64_t nrot, int64_t rot_offset,
+            float *out_lcc, int32_t *out_rot, int flags);
+
+/* Resident variant (inputs and outputs stay in device memory):
+ * upload a rotation set once, scan slices of it, read the results. */
+int pf_set_rotations(pf_ctx *ctx, const double *rotmats, int64_t nrot);
+int pf_reset_results(pf_ctx *ctx);
+int pf_scan_resident(pf_ctx *ctx, int64_t first, int64_t count, int64_t rot_offset, int flags);
+int pf_get_results(pf_ctx *ctx, float *out_lcc, int32_t *out_rot);
+int pf_synchronize(pf_ctx *ctx);
+
+/* Tuning: rotation pairs per batch, rows per tile of passes 1 and 3
+ * (0 keeps the current value). */
+int pf_set_tuning(pf_ctx *ctx, int pairs_per_batch, int rows_pass1, int rows_pass3);
+int pf_get_tuning(const pf_ctx *ctx, int *pairs_per_batch, int *rows_pass1, int *rows_pass3);
+/* Radius beyond which rotated data is zero (pruning), planes kept, rmax. */
+int pf_get_geometry(const pf_ctx *ctx, int *reff, int *valid_planes, int *rmax);
+
+/* Kernel timing (CUDA events around every launch while enabled):
+ * accumulated milliseconds and launch counts of pass 1, 2, 3. */
+int pf_set_profiling(pf_ctx *ctx, int enable);
+int pf_get_kernel_times(pf_ctx *ctx, double *ms, int64_t *launches);
+
+/* Diagnostic: forward 3D FFT of a real grid through the library's own
+ * transforms; out = (nz, ny, nx) complex64 interleaved in natural order.
+ * No reference counterpart (the reference calls FFTW / clFFT). */
+int pf_fft3d(pf_ctx *ctx, const float *in, float *out);
+
+/* --- unit-level mirrors of the reference's native helpers (run on the
+ *     current CUDA device) -------------------------------------------------- */
+/* _extensions.c:7-196: out[p] = grid(R^T p) for |p| <= radius, periodic wrap;
+ * trilinear (nearest == 0) or nearest; voxels outside the sphere untouched. */
+int pf_rotate_grid3d(const double *grid, int nz, int ny, int nx, const double *rotmat,
+                     int radius, double *out, int nearest);
+/* _powerfit.pyx:45-53: out = conj(in1) * in2, n complex128 (interleaved). */
+int pf_conj_multiply(const double *in1, const double *in2, double *out, int64_t n);
+/* _powerfit.pyx:56-72: lcc = gcc / sqrt(ave2 - ave^2) where mask != 0. */
+int pf_calc_lcc(const double *gcc, const double *ave, const double *ave2, const uint8_t *mask,
+                double *lcc, int64_t n);
+/* powerfitter.py:146-163: merge one rotation shard into (lcc, rot):
+ * where part_lcc > lcc: lcc = part_lcc, rot = part_rot + rot_add. */
+int pf_combine(float *lcc, int32_t *rot, const float *part_lcc, const int32_t *part_rot,
+               int64_t n, int64_t rot_add);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* POWERFIT_GB300_H */

@@ -1,0 +1,265 @@
+"""ctypes binding of ``libpowerfit_gb300.so`` (C ABI in ``include/powerfit_gb300.h``).
+
+There is no CPU fallback: if the library is missing or cannot be loaded every
+call raises ``NativeLibraryError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libpowerfit_gb300.so")
+
+PF_FLAG_FP64_NORM = 1
+PF_FLAG_NO_PRUNE = 2
+PF_FLAG_ACCUMULATE = 4
+
+EXPORTS = [
+    "pf_create", "pf_destroy", "pf_last_error", "pf_global_error", "pf_set_target",
+    "pf_set_template_mask", "pf_scan", "pf_set_rotations", "pf_reset_results",
+    "pf_scan_resident", "pf_get_results", "pf_synchronize", "pf_set_tuning", "pf_get_tuning",
+    "pf_get_geometry", "pf_set_profiling", "pf_get_kernel_times", "pf_fft3d",
+    "pf_rotate_grid3d", "pf_conj_multiply", "pf_calc_lcc", "pf_combine",
+]
+
+
+class NativeLibraryError(RuntimeError):
+    pass
+
+
+class PowerFitError(RuntimeError):
+    """A C-ABI call returned an error status."""
+
+    def __init__(self, code, msg):
+        super().__init__("%s (status %d)" % (msg, code))
+        self.code = code
+
+
+_lock = threading.Lock()
+_lib = None
+
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_i64 = ctypes.c_int64
+_d = ctypes.c_double
+_sz = ctypes.c_size_t
+
+
+def load(path=None):
+    """Load the shared library (once) and declare its signatures."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = path or LIB_PATH
+        if not os.path.exists(path):
+            raise NativeLibraryError(
+                "libpowerfit_gb300.so not built: run powerfit_gb300.build.build() "
+                "(or __graft_entry__.build()) first; there is no CPU fallback")
+        try:
+            lib = ctypes.CDLL(path)
+        except OSError as e:
+            raise NativeLibraryError("cannot load %s: %s" % (path, e)) from e
+        sig = {
+            "pf_create": (_vp, [_i, _i, _i, _i, ctypes.POINTER(_i)]),
+            "pf_destroy": (_i, [_vp]),
+            "pf_last_error": (_i, [_vp, ctypes.c_char_p, _sz]),
+            "pf_global_error": (_i, [ctypes.c_char_p, _sz]),
+            "pf_set_target": (_i, [_vp, _vp, _vp]),
+            "pf_set_template_mask": (_i, [_vp, _vp, _vp, _d, _i]),
+            "pf_scan": (_i, [_vp, _vp, _i64, _i64, _vp, _vp, _i]),
+            "pf_set_rotations": (_i, [_vp, _vp, _i64]),
+            "pf_reset_results": (_i, [_vp]),
+            "pf_scan_resident": (_i, [_vp, _i64, _i64, _i64, _i]),
+            "pf_get_results": (_i, [_vp, _vp, _vp]),
+            "pf_synchronize": (_i, [_vp]),
+            "pf_set_tuning": (_i, [_vp, _i, _i, _i]),
+            "pf_get_tuning": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+            "pf_get_geometry": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+            "pf_set_profiling": (_i, [_vp, _i]),
+            "pf_get_kernel_times": (_i, [_vp, _vp, _vp]),
+            "pf_fft3d": (_i, [_vp, _vp, _vp]),
+            "pf_rotate_grid3d": (_i, [_vp, _i, _i, _i, _vp, _i, _vp, _i]),
+            "pf_conj_multiply": (_i, [_vp, _vp, _vp, _i64]),
+            "pf_calc_lcc": (_i, [_vp, _vp, _vp, _vp, _vp, _i64]),
+            "pf_combine": (_i, [_vp, _vp, _vp, _vp, _i64, _i64]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def global_error():
+    buf = ctypes.create_string_buffer(512)
+    load().pf_global_error(buf, 512)
+    return buf.value.decode(errors="replace")
+
+
+def check(rc, ctx=None):
+    if rc != 0:
+        buf = ctypes.create_string_buffer(512)
+        load().pf_last_error(ctx, buf, 512)
+        raise PowerFitError(rc, buf.value.decode(errors="replace"))
+
+
+def ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def c64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None and a.shape != tuple(shape):
+        raise ValueError("expected shape %s, got %s" % (tuple(shape), a.shape))
+    return a
+
+
+class Context:
+    """Owns one ``pf_ctx`` (one grid shape on one device)."""
+
+    def __init__(self, shape, device=0):
+        lib = load()
+        nz, ny, nx = (int(s) for s in shape)
+        st = ctypes.c_int(0)
+        h = lib.pf_create(nz, ny, nx, int(device), ctypes.byref(st))
+        if not h:
+            raise PowerFitError(st.value, global_error())
+        self._h = ctypes.c_void_p(h)
+        self.shape = (nz, ny, nx)
+        self.device = int(device)
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise PowerFitError(-4, "context destroyed")
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            load().pf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _call(self, name, *args):
+        check(getattr(load(), name)(self.handle, *args), self.handle)
+
+    def set_target(self, target, lcc_mask):
+        t = c64(target, self.shape)
+        m = np.ascontiguousarray(lcc_mask, dtype=np.uint8)
+        if m.shape != self.shape:
+            raise ValueError("lcc mask shape mismatch")
+        self._call("pf_set_target", ptr(t), ptr(m))
+
+    def set_template_mask(self, template, mask, norm_factor, rmax):
+        t = c64(template, self.shape)
+        m = c64(mask, self.shape)
+        self._call("pf_set_template_mask", ptr(t), ptr(m), float(norm_factor), int(rmax))
+
+    def scan(self, rotmats, rot_offset=0, flags=0):
+        r = np.ascontiguousarray(rotmats, dtype=np.float64).reshape(-1, 9)
+        lcc = np.empty(self.shape, dtype=np.float32)
+        rot = np.empty(self.shape, dtype=np.int32)
+        self._call("pf_scan", ptr(r), r.shape[0], int(rot_offset), ptr(lcc), ptr(rot), int(flags))
+        return lcc, rot
+
+    def set_rotations(self, rotmats):
+        r = np.ascontiguousarray(rotmats, dtype=np.float64).reshape(-1, 9)
+        self._call("pf_set_rotations", ptr(r), r.shape[0])
+        return r.shape[0]
+
+    def reset_results(self):
+        self._call("pf_reset_results")
+
+    def scan_resident(self, first, count, rot_offset=0, flags=0):
+        self._call("pf_scan_resident", int(first), int(count), int(rot_offset), int(flags))
+
+    def get_results(self, out_lcc=None, out_rot=None):
+        lcc = out_lcc if out_lcc is not None else np.empty(self.shape, dtype=np.float32)
+        rot = out_rot if out_rot is not None else np.empty(self.shape, dtype=np.int32)
+        self._call("pf_get_results", ptr(lcc), ptr(rot))
+        return lcc, rot
+
+    def synchronize(self):
+        self._call("pf_synchronize")
+
+    def set_tuning(self, pairs=0, rows1=0, rows3=0):
+        self._call("pf_set_tuning", int(pairs), int(rows1), int(rows3))
+
+    def get_tuning(self):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._call("pf_get_tuning", ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return a.value, b.value, c.value
+
+    def get_geometry(self):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._call("pf_get_geometry", ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return dict(reff=a.value, valid_planes=b.value, rmax=c.value)
+
+    def set_profiling(self, enable):
+        self._call("pf_set_profiling", int(bool(enable)))
+
+    def kernel_times(self):
+        ms = np.zeros(3, dtype=np.float64)
+        n = np.zeros(3, dtype=np.int64)
+        self._call("pf_get_kernel_times", ptr(ms), ptr(n))
+        return ms, n
+
+    def fft3d(self, real):
+        a = np.ascontiguousarray(real, dtype=np.float32)
+        if a.shape != self.shape:
+            raise ValueError("shape mismatch")
+        out = np.empty(self.shape, dtype=np.complex64)
+        self._call("pf_fft3d", ptr(a), ptr(out))
+        return out
+
+
+# ---- unit-level mirrors ----------------------------------------------------
+
+def rotate_grid3d(grid, rotmat, radius, out, nearest):
+    """GPU mirror of ``_extensions.rotate_grid3d`` (writes ``out`` in place)."""
+    g = c64(grid)
+    if out.dtype != np.float64 or not out.flags.c_contiguous or out.shape != g.shape:
+        raise ValueError("out must be a C-contiguous float64 array of the grid's shape")
+    r = c64(rotmat).reshape(9)
+    nz, ny, nx = g.shape
+    check(load().pf_rotate_grid3d(ptr(g), nz, ny, nx, ptr(r), int(radius), ptr(out), int(bool(nearest))))
+    return out
+
+
+def conj_multiply(in1, in2, out):
+    a = np.ascontiguousarray(in1, dtype=np.complex128)
+    b = np.ascontiguousarray(in2, dtype=np.complex128)
+    if out.dtype != np.complex128 or not out.flags.c_contiguous or out.size != a.size or b.size != a.size:
+        raise ValueError("conj_multiply: size/dtype mismatch")
+    check(load().pf_conj_multiply(ptr(a), ptr(b), ptr(out), a.size))
+    return out
+
+
+def calc_lcc(gcc, ave, ave2, mask, lcc):
+    g, a, a2 = (np.ascontiguousarray(x, dtype=np.float64) for x in (gcc, ave, ave2))
+    m = np.ascontiguousarray(mask, dtype=np.uint8)
+    if lcc.dtype != np.float64 or not lcc.flags.c_contiguous or not (g.size == a.size == a2.size == m.size == lcc.size):
+        raise ValueError("calc_lcc: size/dtype mismatch")
+    check(load().pf_calc_lcc(ptr(g), ptr(a), ptr(a2), ptr(m), ptr(lcc), g.size))
+    return lcc
+
+
+def combine_into(lcc, rot, part_lcc, part_rot, rot_add):
+    """GPU merge of one rotation shard (``PowerFitter._combine`` semantics)."""
+    pl = np.ascontiguousarray(part_lcc, dtype=np.float32)
+    pr = np.ascontiguousarray(part_rot, dtype=np.int32)
+    if lcc.dtype != np.float32 or rot.dtype != np.int32 or lcc.size != pl.size or rot.size != pr.size:
+        raise ValueError("combine: dtype/size mismatch")
+    check(load().pf_combine(ptr(lcc), ptr(rot), ptr(pl), ptr(pr), lcc.size, int(rot_add)))
+    return lcc, rot

@@ -1,0 +1,797 @@
+// C ABI of the GB300 LCC search: context, device memory, launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <functional>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/powerfit_gb300.h"
+#include "pf_kernels.cuh"
+
+using namespace pf;
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+void set_global_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+// Factor n into Stockham radices: fewest stages, then the largest smallest radix.
+bool make_plan(int n, AxisPlan* pl) {
+  static const int radices[] = {16, 12, 10, 8, 7, 6, 5, 4, 3, 2};
+  std::vector<int> best, cur;
+  int best_min = 0;
+  auto consider = [&]() {
+    int mn = *std::min_element(cur.begin(), cur.end());
+    if (best.empty() || cur.size() < best.size() || (cur.size() == best.size() && mn > best_min)) {
+      best = cur;
+      best_min = mn;
+    }
+  };
+  std::function<void(int, int)> rec = [&](int rem, int maxr) {
+    if (rem == 1) {
+      if (!cur.empty()) consider();
+      return;
+    }
+    if (!best.empty() && cur.size() + 1 > best.size()) return;
+    for (int r : radices) {
+      if (r > maxr || rem % r) continue;
+      cur.push_back(r);
+      rec(rem / r, r);
+      cur.pop_back();
+    }
+  };
+  if (n == 1) {
+    pl->n = 1;
+    pl->nst = 1;
+    pl->radix[0] = 1;
+    return true;
+  }
+  rec(n, 16);
+  if (best.empty() || (int)best.size() > kMaxStages) return false;
+  pl->n = n;
+  pl->nst = (int)best.size();
+  for (int i = 0; i < pl->nst; ++i) pl->radix[i] = best[i];
+  return true;
+}
+
+std::vector<float2> twiddles(int n) {
+  std::vector<float2> t(n);
+  for (int m = 0; m < n; ++m) {
+    const double a = 2.0 * M_PI * (double)m / (double)n;
+    t[m] = make_float2((float)std::cos(a), (float)-std::sin(a));
+  }
+  return t;
+}
+
+RotFixed to_fixed(const double* r) {
+  RotFixed f;
+  for (int i = 0; i < 9; ++i) f.r[i] = (long long)std::llround(r[i] * 4294967296.0);
+  return f;
+}
+
+size_t line_smem(int X, int nf, int ty) { return ((size_t)X + (size_t)nf * ty * (X + kPad)) * sizeof(float2); }
+size_t plane_smem(int Y, int Z) { return ((size_t)Y + Z + (size_t)Z * (Y + kPad)) * sizeof(float2); }
+
+}  // namespace
+
+struct pf_ctx {
+  int device = 0;
+  int nz = 0, ny = 0, nx = 0;
+  long long N = 0;
+  cudaStream_t stream = nullptr;
+  AxisPlan px{}, py{}, pz{};
+  float2 *twx = nullptr, *twy = nullptr, *twz = nullptr;
+  float *tmpl = nullptr, *mask = nullptr;
+  unsigned char* lcc_mask = nullptr;
+  float2* spec = nullptr;          // [2][kx][kz][ky]
+  float* lcc = nullptr;
+  int* rot = nullptr;
+  float2* buf = nullptr;
+  long long buf_pairs = 0;
+  RotFixed* rots = nullptr;
+  double* rotd = nullptr;
+  long long nrot = 0, rot_cap = 0;
+  Geometry g{};
+  int rmax = 0, reff_data = 0;
+  float norm_factor = 0.f;
+  bool have_target = false, have_template = false;
+  int pairs = 1, ty1 = 16, ty3 = 16;
+  size_t max_smem = 0;
+  bool profiling = false;
+  double ms[3] = {0, 0, 0};
+  long long launches[3] = {0, 0, 0};
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  char err[512] = "";
+};
+
+namespace {
+
+int fail(pf_ctx* c, int code, const char* fmt, ...) {
+  char tmp[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(tmp, sizeof(tmp), fmt, ap);
+  va_end(ap);
+  if (c) snprintf(c->err, sizeof(c->err), "%s", tmp);
+  snprintf(g_err, sizeof(g_err), "%s", tmp);
+  return code;
+}
+
+#define PF_CUDA(c, call)                                                                            \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) return fail((c), PF_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                       __FILE__, __LINE__);                                         \
+  } while (0)
+
+int alloc(pf_ctx* c, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(c, PF_E_NOMEM, "cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+  }
+  return PF_OK;
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+void choose_tiles(pf_ctx* c) {
+  const int X = c->nx;
+  int ty = 16;
+  while (ty > 1 && ((long long)ty * X > (long long)kMaxVoxPerThread * kThreadsLine || line_smem(X, 3, ty) > 96 * 1024)) ty--;
+  c->ty1 = ty;
+  // pass 3: enough tiles to fill the machine (>= 4 per SM on 152 SMs)
+  int ty3 = ty;
+  while (ty3 > 2 && (long long)c->nz * ((c->ny + ty3 - 1) / ty3) < 4 * 152) ty3 /= 2;
+  c->ty3 = ty3;
+  // pairs per batch: intermediate spectra of one batch <= 64 MiB (L2-sized), at least 1, at most 16
+  const long long per_pair = 3LL * c->N * (long long)sizeof(float2);
+  long long p = (64LL << 20) / per_pair;
+  c->pairs = (int)std::max(1LL, std::min(16LL, p));
+}
+
+int ensure_buf(pf_ctx* c, int pairs) {
+  if (c->buf && c->buf_pairs >= pairs) return PF_OK;
+  if (c->buf) cudaFree(c->buf);
+  c->buf = nullptr;
+  c->buf_pairs = 0;
+  int rc = alloc(c, (void**)&c->buf, (size_t)pairs * 3 * c->N * sizeof(float2));
+  if (rc) return rc;
+  c->buf_pairs = pairs;
+  return PF_OK;
+}
+
+void compute_geometry(pf_ctx* c, int reff) {
+  Geometry& g = c->g;
+  g.nz = c->nz;
+  g.ny = c->ny;
+  g.nx = c->nx;
+  g.rmax = c->rmax;
+  g.reff = reff;
+  const int re = std::min(c->rmax, reff);
+  if (2 * re + 1 >= c->nz) {
+    g.nvz = c->nz;
+    g.zlo = c->nz - 1;
+  } else {
+    g.nvz = 2 * re + 1;
+    g.zlo = re;
+  }
+}
+
+cudaEvent_t get_event(pf_ctx* c) {
+  if (!c->ev_pool.empty()) {
+    cudaEvent_t e = c->ev_pool.back();
+    c->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void collect_events(pf_ctx* c) {
+  for (auto& pe : c->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, pe.second.first, pe.second.second) == cudaSuccess) {
+      c->ms[pe.first] += ms;
+      c->launches[pe.first] += 1;
+    }
+    c->ev_pool.push_back(pe.second.first);
+    c->ev_pool.push_back(pe.second.second);
+  }
+  c->pending.clear();
+}
+
+template <class Launch>
+int timed_launch(pf_ctx* c, int which, Launch&& launch) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (c->profiling) {
+    a = get_event(c);
+    b = get_event(c);
+    cudaEventRecord(a, c->stream);
+  }
+  launch();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(c, PF_E_CUDA, "kernel launch (pass %d) failed: %s", which + 1, cudaGetErrorString(e));
+  if (c->profiling) {
+    cudaEventRecord(b, c->stream);
+    c->pending.push_back({which, {a, b}});
+    if (c->pending.size() > 4096) {
+      cudaEventSynchronize(b);
+      collect_events(c);
+    }
+  }
+  return PF_OK;
+}
+
+int set_smem_limits(pf_ctx* c) {
+  const size_t s1 = line_smem(c->nx, 3, 16);
+  const size_t s2 = plane_smem(c->ny, c->nz);
+  PF_CUDA(c, cudaFuncSetAttribute(k_pass1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(s1, (size_t)48 * 1024)));
+  PF_CUDA(c, cudaFuncSetAttribute(k_pass3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(s1, (size_t)48 * 1024)));
+  PF_CUDA(c, cudaFuncSetAttribute(k_fwd_x_real, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(s1, (size_t)48 * 1024)));
+  PF_CUDA(c, cudaFuncSetAttribute(k_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
+  return PF_OK;
+}
+
+int upload_double_as_float(pf_ctx* c, float* dst, const double* src, long long n) {
+  std::vector<float> tmp((size_t)n);
+  for (long long i = 0; i < n; ++i) tmp[i] = (float)src[i];
+  PF_CUDA(c, cudaMemcpyAsync(dst, tmp.data(), n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  PF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PF_OK;
+}
+
+// forward transforms of two real device fields -> spectra [2][kx][kz][ky] * scale
+int forward_two_fields(pf_ctx* c, const float* in0, const float* in1, int square1, float2* out, float scale) {
+  int rc = ensure_buf(c, 1);
+  if (rc) return rc;
+  Geometry gfull = c->g;
+  gfull.nvz = c->nz;
+  gfull.zlo = c->nz - 1;
+  const int ty = c->ty1;
+  FwdXParams fx{gfull, c->px, c->twx, in0, in1, square1, c->buf, ty};
+  dim3 g1(c->nz, (c->ny + ty - 1) / ty, 1);
+  k_fwd_x_real<<<g1, kThreadsLine, line_smem(c->nx, 3, ty), c->stream>>>(fx);
+  PF_CUDA(c, cudaGetLastError());
+  Pass2Params p2{};
+  p2.g = gfull;
+  p2.py = c->py;
+  p2.pz = c->pz;
+  p2.twy = c->twy;
+  p2.twz = c->twz;
+  p2.buf = c->buf;
+  p2.nfield = 2;
+  p2.mode = 1;
+  p2.out = out;
+  p2.scale = scale;
+  dim3 g2(c->nx, 2, 1);
+  k_pass2<<<g2, kThreadsPlane, plane_smem(c->ny, c->nz), c->stream>>>(p2);
+  PF_CUDA(c, cudaGetLastError());
+  PF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pf_global_error(char* buf, size_t len) {
+  if (!buf || !len) return PF_E_ARG;
+  snprintf(buf, len, "%s", g_err);
+  return PF_OK;
+}
+
+int pf_last_error(const pf_ctx* ctx, char* buf, size_t len) {
+  if (!buf || !len) return PF_E_ARG;
+  snprintf(buf, len, "%s", ctx ? ctx->err : g_err);
+  return PF_OK;
+}
+
+pf_ctx* pf_create(int nz, int ny, int nx, int device, int* status) {
+  auto ret = [&](int code) -> pf_ctx* {
+    if (status) *status = code;
+    return nullptr;
+  };
+  if (nz < 1 || ny < 1 || nx < 1) {
+    set_global_error("grid shape must be positive, got (%d, %d, %d)", nz, ny, nx);
+    return ret(PF_E_ARG);
+  }
+  if (nz > 2048 || ny > 2048 || nx > 2048) {
+    set_global_error("grid edges are limited to 2048, got (%d, %d, %d)", nz, ny, nx);
+    return ret(PF_E_SHAPE);
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    set_global_error("CUDA device %d not available (%d devices)", device, ndev);
+    return ret(PF_E_CUDA);
+  }
+  DeviceGuard guard(device);
+  pf_ctx* c = new pf_ctx();
+  c->device = device;
+  c->nz = nz;
+  c->ny = ny;
+  c->nx = nx;
+  c->N = (long long)nz * ny * nx;
+  if (!make_plan(nx, &c->px) || !make_plan(ny, &c->py) || !make_plan(nz, &c->pz)) {
+    set_global_error("grid (%d, %d, %d): every edge must factor into 2, 3, 5 and 7", nz, ny, nx);
+    delete c;
+    return ret(PF_E_SHAPE);
+  }
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, device);
+  c->max_smem = prop.sharedMemPerBlockOptin;
+  if (plane_smem(ny, nz) > c->max_smem) {
+    set_global_error("grid (%d, %d, %d): a (z, y) plane needs %zu bytes of shared memory, the device offers %zu",
+                     nz, ny, nx, plane_smem(ny, nz), c->max_smem);
+    delete c;
+    return ret(PF_E_SHAPE);
+  }
+  c->rmax = std::min(nz, std::min(ny, nx)) / 2;
+  choose_tiles(c);
+  int rc = PF_OK;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) rc = PF_E_CUDA;
+  const size_t N = (size_t)c->N;
+  if (!rc) rc = alloc(c, (void**)&c->twx, nx * sizeof(float2));
+  if (!rc) rc = alloc(c, (void**)&c->twy, ny * sizeof(float2));
+  if (!rc) rc = alloc(c, (void**)&c->twz, nz * sizeof(float2));
+  if (!rc) rc = alloc(c, (void**)&c->tmpl, N * sizeof(float));
+  if (!rc) rc = alloc(c, (void**)&c->mask, N * sizeof(float));
+  if (!rc) rc = alloc(c, (void**)&c->lcc_mask, N);
+  if (!rc) rc = alloc(c, (void**)&c->spec, 2 * N * sizeof(float2));
+  if (!rc) rc = alloc(c, (void**)&c->lcc, N * sizeof(float));
+  if (!rc) rc = alloc(c, (void**)&c->rot, N * sizeof(int));
+  if (!rc) rc = ensure_buf(c, c->pairs);
+  if (!rc) {
+    auto tx = twiddles(nx), ty = twiddles(ny), tz = twiddles(nz);
+    if (cudaMemcpy(c->twx, tx.data(), nx * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(c->twy, ty.data(), ny * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(c->twz, tz.data(), nz * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = fail(c, PF_E_CUDA, "twiddle upload failed");
+  }
+  if (!rc) rc = set_smem_limits(c);
+  if (!rc && (cudaMemset(c->lcc, 0, N * sizeof(float)) != cudaSuccess ||
+              cudaMemset(c->rot, 0, N * sizeof(int)) != cudaSuccess))
+    rc = fail(c, PF_E_CUDA, "memset failed");
+  compute_geometry(c, c->rmax);
+  if (rc) {
+    snprintf(g_err, sizeof(g_err), "%s", c->err);
+    pf_destroy(c);
+    return ret(rc);
+  }
+  if (status) *status = PF_OK;
+  return c;
+}
+
+int pf_destroy(pf_ctx* c) {
+  if (!c) return PF_E_ARG;
+  DeviceGuard guard(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  collect_events(c);
+  for (auto e : c->ev_pool) cudaEventDestroy(e);
+  void* ptrs[] = {c->twx, c->twy, c->twz, c->tmpl, c->mask, c->lcc_mask, c->spec, c->lcc, c->rot, c->buf, c->rots, c->rotd};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return PF_OK;
+}
+
+int pf_set_target(pf_ctx* c, const double* target, const uint8_t* lcc_mask) {
+  if (!c || !target || !lcc_mask) return fail(c, PF_E_ARG, "pf_set_target: null argument");
+  DeviceGuard guard(c->device);
+  const long long N = c->N;
+  float* dt = nullptr;
+  int rc = alloc(c, (void**)&dt, N * sizeof(float));
+  if (rc) return rc;
+  rc = upload_double_as_float(c, dt, target, N);
+  if (!rc && cudaMemcpy(c->lcc_mask, lcc_mask, N, cudaMemcpyHostToDevice) != cudaSuccess)
+    rc = fail(c, PF_E_CUDA, "lcc mask upload failed");
+  if (!rc) rc = forward_two_fields(c, dt, nullptr, 1, c->spec, (float)(1.0 / (double)N));
+  cudaFree(dt);
+  if (!rc) c->have_target = true;
+  return rc;
+}
+
+int pf_set_template_mask(pf_ctx* c, const double* tmpl, const double* mask, double norm_factor, int rmax) {
+  if (!c || !tmpl || !mask) return fail(c, PF_E_ARG, "pf_set_template_mask: null argument");
+  if (!(norm_factor > 0)) return fail(c, PF_E_ARG, "norm_factor must be positive (zero-filled mask)");
+  if (rmax < 0 || 2 * rmax > std::min(c->nz, std::min(c->ny, c->nx)))
+    return fail(c, PF_E_ARG, "rmax %d outside [0, min(shape)//2]", rmax);
+  DeviceGuard guard(c->device);
+  int rc = upload_double_as_float(c, c->tmpl, tmpl, c->N);
+  if (!rc) rc = upload_double_as_float(c, c->mask, mask, c->N);
+  if (rc) return rc;
+  c->rmax = rmax;
+  c->norm_factor = (float)norm_factor;
+  // radius of the data support (minimal-image distance of any nonzero voxel)
+  double rs2 = -1.0;
+  for (int z = 0; z < c->nz; ++z) {
+    const int cz = (2 * z <= c->nz) ? z : z - c->nz;
+    for (int y = 0; y < c->ny; ++y) {
+      const int cy = (2 * y <= c->ny) ? y : y - c->ny;
+      const long long row = ((long long)z * c->ny + y) * c->nx;
+      for (int x = 0; x < c->nx; ++x) {
+        if (tmpl[row + x] != 0.0 || mask[row + x] != 0.0) {
+          const int cx = (2 * x <= c->nx) ? x : x - c->nx;
+          const double d2 = (double)cz * cz + (double)cy * cy + (double)cx * cx;
+          if (d2 > rs2) rs2 = d2;
+        }
+      }
+    }
+  }
+  const int nmin = std::min(c->nz, std::min(c->ny, c->nx));
+  const double rs = rs2 < 0 ? 0.0 : std::sqrt(rs2);
+  // a rotated sample at |p| > rs + sqrt(3) only touches voxels farther than rs
+  // (as long as the support stays clear of the periodic boundary)
+  int reff = rmax;
+  if (rs + 1.0 < nmin / 2.0) reff = std::min(rmax, (int)std::floor(rs + 1.7320508075688772 + 1e-6) + 1);
+  c->reff_data = reff;
+  compute_geometry(c, reff);
+  c->have_template = true;
+  return PF_OK;
+}
+
+int pf_set_rotations(pf_ctx* c, const double* rotmats, int64_t nrot) {
+  if (!c || (!rotmats && nrot > 0) || nrot < 0) return fail(c, PF_E_ARG, "pf_set_rotations: bad arguments");
+  if (nrot > (int64_t)0x7fffffff) return fail(c, PF_E_ARG, "too many rotations");
+  DeviceGuard guard(c->device);
+  if (nrot > c->rot_cap) {
+    if (c->rots) cudaFree(c->rots);
+    if (c->rotd) cudaFree(c->rotd);
+    c->rots = nullptr;
+    c->rotd = nullptr;
+    c->rot_cap = 0;
+    int rc = alloc(c, (void**)&c->rots, std::max<int64_t>(nrot, 1) * sizeof(RotFixed));
+    if (!rc) rc = alloc(c, (void**)&c->rotd, std::max<int64_t>(nrot, 1) * 9 * sizeof(double));
+    if (rc) return rc;
+    c->rot_cap = nrot;
+  }
+  std::vector<RotFixed> fx((size_t)nrot);
+  for (int64_t i = 0; i < nrot; ++i) {
+    for (int k = 0; k < 9; ++k)
+      if (!std::isfinite(rotmats[9 * i + k]) || std::fabs(rotmats[9 * i + k]) > 2.0)
+        return fail(c, PF_E_ARG, "rotation %lld element %d is not a rotation-matrix entry", (long long)i, k);
+    fx[i] = to_fixed(rotmats + 9 * i);
+  }
+  if (nrot > 0) {
+    PF_CUDA(c, cudaMemcpyAsync(c->rots, fx.data(), nrot * sizeof(RotFixed), cudaMemcpyHostToDevice, c->stream));
+    PF_CUDA(c, cudaMemcpyAsync(c->rotd, rotmats, nrot * 9 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    PF_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  c->nrot = nrot;
+  return PF_OK;
+}
+
+int pf_reset_results(pf_ctx* c) {
+  if (!c) return PF_E_ARG;
+  DeviceGuard guard(c->device);
+  PF_CUDA(c, cudaMemsetAsync(c->lcc, 0, c->N * sizeof(float), c->stream));
+  PF_CUDA(c, cudaMemsetAsync(c->rot, 0, c->N * sizeof(int), c->stream));
+  return PF_OK;
+}
+
+int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset, int flags) {
+  if (!c) return fail(c, PF_E_ARG, "null context");
+  if (!c->have_target || !c->have_template) return fail(c, PF_E_STATE, "set the target and the template/mask first");
+  if (first < 0 || count < 0 || first + count > c->nrot) return fail(c, PF_E_ARG, "rotation range outside the uploaded set");
+  if (rot_offset + first + count > (int64_t)0x7fffffff) return fail(c, PF_E_ARG, "rotation index overflows int32");
+  DeviceGuard guard(c->device);
+  int rc = ensure_buf(c, c->pairs);
+  if (rc) return rc;
+  if (!(flags & PF_FLAG_ACCUMULATE)) {
+    rc = pf_reset_results(c);
+    if (rc) return rc;
+  }
+  Geometry g = c->g;
+  if (flags & PF_FLAG_NO_PRUNE) {
+    Geometry full = g;
+    full.reff = c->rmax;
+    const int re = c->rmax;
+    if (2 * re + 1 >= c->nz) { full.nvz = c->nz; full.zlo = c->nz - 1; }
+    else { full.nvz = 2 * re + 1; full.zlo = re; }
+    g = full;
+  }
+  const int P = c->pairs;
+  const int ty1 = c->ty1, ty3 = c->ty3;
+  const size_t s1 = line_smem(c->nx, 3, ty1), s3 = line_smem(c->nx, 3, ty3), s2 = plane_smem(c->ny, c->nz);
+  const int64_t end = first + count;
+  for (int64_t r0 = first; r0 < end; r0 += 2LL * P) {
+    const int npairs = (int)std::min<int64_t>(P, (end - r0 + 1) / 2);
+    Pass1Params p1{g, c->px, GatherSrc{c->tmpl, c->mask}, c->twx, c->rots, c->rotd, r0, end, c->buf, ty1};
+    dim3 g1(g.nvz, (c->ny + ty1 - 1) / ty1, npairs);
+    rc = timed_launch(c, 0, [&] { k_pass1<<<g1, kThreadsLine, s1, c->stream>>>(p1); });
+    if (rc) return rc;
+    Pass2Params p2{};
+    p2.g = g;
+    p2.py = c->py;
+    p2.pz = c->pz;
+    p2.twy = c->twy;
+    p2.twz = c->twz;
+    p2.buf = c->buf;
+    p2.s1 = c->spec;
+    p2.s2 = c->spec + c->N;
+    p2.nfield = 3;
+    p2.mode = 0;
+    dim3 g2(c->nx, 3, npairs);
+    rc = timed_launch(c, 1, [&] { k_pass2<<<g2, kThreadsPlane, s2, c->stream>>>(p2); });
+    if (rc) return rc;
+    Pass3Params p3{g, c->px, c->twx, c->buf, npairs, r0, end, rot_offset, c->lcc_mask, c->norm_factor,
+                   c->lcc, c->rot, ty3, (flags & PF_FLAG_FP64_NORM) ? 1 : 0};
+    dim3 g3(c->nz, (c->ny + ty3 - 1) / ty3, 1);
+    rc = timed_launch(c, 2, [&] { k_pass3<<<g3, kThreadsLine, s3, c->stream>>>(p3); });
+    if (rc) return rc;
+  }
+  return PF_OK;
+}
+
+int pf_get_results(pf_ctx* c, float* out_lcc, int32_t* out_rot) {
+  if (!c || !out_lcc || !out_rot) return fail(c, PF_E_ARG, "pf_get_results: null argument");
+  DeviceGuard guard(c->device);
+  PF_CUDA(c, cudaMemcpyAsync(out_lcc, c->lcc, c->N * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  PF_CUDA(c, cudaMemcpyAsync(out_rot, c->rot, c->N * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  PF_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (c->profiling) collect_events(c);
+  return PF_OK;
+}
+
+int pf_synchronize(pf_ctx* c) {
+  if (!c) return PF_E_ARG;
+  DeviceGuard guard(c->device);
+  PF_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (c->profiling) collect_events(c);
+  return PF_OK;
+}
+
+int pf_scan(pf_ctx* c, const double* rotmats, int64_t nrot, int64_t rot_offset, float* out_lcc, int32_t* out_rot,
+            int flags) {
+  if (!c) return fail(c, PF_E_ARG, "null context");
+  int rc = pf_set_rotations(c, rotmats, nrot);
+  if (!rc) rc = pf_scan_resident(c, 0, nrot, rot_offset, flags & ~PF_FLAG_ACCUMULATE);
+  if (!rc) rc = pf_get_results(c, out_lcc, out_rot);
+  return rc;
+}
+
+int pf_set_tuning(pf_ctx* c, int pairs, int rows1, int rows3) {
+  if (!c) return PF_E_ARG;
+  if (pairs < 0 || rows1 < 0 || rows3 < 0) return fail(c, PF_E_ARG, "tuning values must be >= 0");
+  auto ok_rows = [&](int ty) {
+    return (long long)ty * c->nx <= (long long)kMaxVoxPerThread * kThreadsLine &&
+           line_smem(c->nx, 3, ty) <= std::max(line_smem(c->nx, 3, 16), (size_t)48 * 1024);
+  };
+  if (rows1 && !ok_rows(rows1)) return fail(c, PF_E_ARG, "rows_pass1 %d too large for nx %d", rows1, c->nx);
+  if (rows3 && !ok_rows(rows3)) return fail(c, PF_E_ARG, "rows_pass3 %d too large for nx %d", rows3, c->nx);
+  if (pairs) {
+    DeviceGuard guard(c->device);
+    cudaStreamSynchronize(c->stream);
+    int rc = ensure_buf(c, pairs);
+    if (rc) return rc;
+    c->pairs = pairs;
+  }
+  if (rows1) c->ty1 = rows1;
+  if (rows3) c->ty3 = rows3;
+  return PF_OK;
+}
+
+int pf_get_tuning(const pf_ctx* c, int* pairs, int* rows1, int* rows3) {
+  if (!c) return PF_E_ARG;
+  if (pairs) *pairs = c->pairs;
+  if (rows1) *rows1 = c->ty1;
+  if (rows3) *rows3 = c->ty3;
+  return PF_OK;
+}
+
+int pf_get_geometry(const pf_ctx* c, int* reff, int* valid_planes, int* rmax) {
+  if (!c) return PF_E_ARG;
+  if (reff) *reff = c->g.reff;
+  if (valid_planes) *valid_planes = c->g.nvz;
+  if (rmax) *rmax = c->rmax;
+  return PF_OK;
+}
+
+int pf_set_profiling(pf_ctx* c, int enable) {
+  if (!c) return PF_E_ARG;
+  DeviceGuard guard(c->device);
+  cudaStreamSynchronize(c->stream);
+  collect_events(c);
+  c->profiling = enable != 0;
+  for (int i = 0; i < 3; ++i) {
+    c->ms[i] = 0;
+    c->launches[i] = 0;
+  }
+  return PF_OK;
+}
+
+int pf_get_kernel_times(pf_ctx* c, double* ms, int64_t* launches) {
+  if (!c || !ms || !launches) return PF_E_ARG;
+  DeviceGuard guard(c->device);
+  cudaStreamSynchronize(c->stream);
+  collect_events(c);
+  for (int i = 0; i < 3; ++i) {
+    ms[i] = c->ms[i];
+    launches[i] = c->launches[i];
+  }
+  return PF_OK;
+}
+
+int pf_fft3d(pf_ctx* c, const float* in, float* out) {
+  if (!c || !in || !out) return fail(c, PF_E_ARG, "pf_fft3d: null argument");
+  DeviceGuard guard(c->device);
+  const long long N = c->N;
+  float* din = nullptr;
+  float2* dout = nullptr;
+  int rc = alloc(c, (void**)&din, N * sizeof(float));
+  if (!rc) rc = alloc(c, (void**)&dout, 2 * N * sizeof(float2));
+  if (!rc && cudaMemcpy(din, in, N * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+    rc = fail(c, PF_E_CUDA, "upload failed");
+  if (!rc) rc = forward_two_fields(c, din, nullptr, 0, dout, 1.0f);
+  std::vector<float2> h;
+  if (!rc) {
+    h.resize((size_t)N);
+    if (cudaMemcpy(h.data(), dout, N * sizeof(float2), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = fail(c, PF_E_CUDA, "download failed");
+  }
+  if (!rc) {
+    // device layout [kx][kz][ky] -> natural [kz][ky][kx]
+    for (int kx = 0; kx < c->nx; ++kx)
+      for (int kz = 0; kz < c->nz; ++kz)
+        for (int ky = 0; ky < c->ny; ++ky) {
+          const float2 v = h[((size_t)kx * c->nz + kz) * c->ny + ky];
+          const size_t o = ((size_t)kz * c->ny + ky) * c->nx + kx;
+          out[2 * o] = v.x;
+          out[2 * o + 1] = v.y;
+        }
+  }
+  if (din) cudaFree(din);
+  if (dout) cudaFree(dout);
+  return rc;
+}
+
+// ----------------------------- unit-level mirrors ---------------------------
+
+int pf_rotate_grid3d(const double* grid, int nz, int ny, int nx, const double* rotmat, int radius, double* out,
+                     int nearest) {
+  if (!grid || !rotmat || !out || nz < 1 || ny < 1 || nx < 1 || radius < 0)
+    return fail(nullptr, PF_E_ARG, "pf_rotate_grid3d: bad arguments");
+  if (radius >= std::min(nz, std::min(ny, nx)))
+    return fail(nullptr, PF_E_ARG, "radius %d must be smaller than every grid edge", radius);
+  const long long N = (long long)nz * ny * nx;
+  float* dg = nullptr;
+  double *dout = nullptr, *drd = nullptr;
+  int rc = alloc(nullptr, (void**)&dg, N * sizeof(float));
+  if (!rc) rc = alloc(nullptr, (void**)&dout, N * sizeof(double));
+  if (!rc) rc = alloc(nullptr, (void**)&drd, 9 * sizeof(double));
+  std::vector<float> hg;
+  if (!rc) {
+    hg.resize((size_t)N);
+    for (long long i = 0; i < N; ++i) hg[i] = (float)grid[i];
+    if (cudaMemcpy(dg, hg.data(), N * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dout, out, N * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(drd, rotmat, 9 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = fail(nullptr, PF_E_CUDA, "upload failed");
+  }
+  if (!rc) {
+    Geometry g{};
+    g.nz = nz;
+    g.ny = ny;
+    g.nx = nx;
+    g.rmax = radius;
+    g.reff = radius;
+    GatherSrc src{dg, dg};
+    k_rotate_grid<<<(unsigned)std::min<long long>((N + 255) / 256, 4096), 256>>>(g, src, to_fixed(rotmat), drd,
+                                                                                radius, nearest, dout);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) rc = fail(nullptr, PF_E_CUDA, "rotate kernel: %s", cudaGetErrorString(e));
+  }
+  if (!rc && cudaMemcpy(out, dout, N * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = fail(nullptr, PF_E_CUDA, "download failed");
+  if (dg) cudaFree(dg);
+  if (dout) cudaFree(dout);
+  if (drd) cudaFree(drd);
+  return rc;
+}
+
+int pf_conj_multiply(const double* in1, const double* in2, double* out, int64_t n) {
+  if (!in1 || !in2 || !out || n < 0) return fail(nullptr, PF_E_ARG, "pf_conj_multiply: bad arguments");
+  if (n == 0) return PF_OK;
+  double2 *a = nullptr, *b = nullptr, *o = nullptr;
+  int rc = alloc(nullptr, (void**)&a, n * sizeof(double2));
+  if (!rc) rc = alloc(nullptr, (void**)&b, n * sizeof(double2));
+  if (!rc) rc = alloc(nullptr, (void**)&o, n * sizeof(double2));
+  if (!rc && (cudaMemcpy(a, in1, n * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess ||
+              cudaMemcpy(b, in2, n * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess))
+    rc = fail(nullptr, PF_E_CUDA, "upload failed");
+  if (!rc) {
+    k_conj_multiply<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256>>>(a, b, o, n);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out, o, n * sizeof(double2), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = fail(nullptr, PF_E_CUDA, "conj_multiply: %s", cudaGetErrorString(e));
+  }
+  if (a) cudaFree(a);
+  if (b) cudaFree(b);
+  if (o) cudaFree(o);
+  return rc;
+}
+
+int pf_calc_lcc(const double* gcc, const double* ave, const double* ave2, const uint8_t* mask, double* lcc,
+                int64_t n) {
+  if (!gcc || !ave || !ave2 || !mask || !lcc || n < 0) return fail(nullptr, PF_E_ARG, "pf_calc_lcc: bad arguments");
+  if (n == 0) return PF_OK;
+  double *dg = nullptr, *da = nullptr, *da2 = nullptr, *dl = nullptr;
+  unsigned char* dm = nullptr;
+  int rc = alloc(nullptr, (void**)&dg, n * sizeof(double));
+  if (!rc) rc = alloc(nullptr, (void**)&da, n * sizeof(double));
+  if (!rc) rc = alloc(nullptr, (void**)&da2, n * sizeof(double));
+  if (!rc) rc = alloc(nullptr, (void**)&dl, n * sizeof(double));
+  if (!rc) rc = alloc(nullptr, (void**)&dm, n);
+  if (!rc && (cudaMemcpy(dg, gcc, n * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+              cudaMemcpy(da, ave, n * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+              cudaMemcpy(da2, ave2, n * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+              cudaMemcpy(dl, lcc, n * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+              cudaMemcpy(dm, mask, n, cudaMemcpyHostToDevice) != cudaSuccess))
+    rc = fail(nullptr, PF_E_CUDA, "upload failed");
+  if (!rc) {
+    k_calc_lcc<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256>>>(dg, da, da2, dm, dl, n);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(lcc, dl, n * 8, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = fail(nullptr, PF_E_CUDA, "calc_lcc: %s", cudaGetErrorString(e));
+  }
+  void* ptrs[] = {dg, da, da2, dl, dm};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  return rc;
+}
+
+int pf_combine(float* lcc, int32_t* rot, const float* part_lcc, const int32_t* part_rot, int64_t n, int64_t rot_add) {
+  if (!lcc || !rot || !part_lcc || !part_rot || n < 0) return fail(nullptr, PF_E_ARG, "pf_combine: bad arguments");
+  if (n == 0) return PF_OK;
+  float *dl = nullptr, *dpl = nullptr;
+  int *dr = nullptr, *dpr = nullptr;
+  int rc = alloc(nullptr, (void**)&dl, n * 4);
+  if (!rc) rc = alloc(nullptr, (void**)&dpl, n * 4);
+  if (!rc) rc = alloc(nullptr, (void**)&dr, n * 4);
+  if (!rc) rc = alloc(nullptr, (void**)&dpr, n * 4);
+  if (!rc && (cudaMemcpy(dl, lcc, n * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+              cudaMemcpy(dpl, part_lcc, n * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+              cudaMemcpy(dr, rot, n * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+              cudaMemcpy(dpr, part_rot, n * 4, cudaMemcpyHostToDevice) != cudaSuccess))
+    rc = fail(nullptr, PF_E_CUDA, "upload failed");
+  if (!rc) {
+    k_combine<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256>>>(dpl, dpr, rot_add, dl, dr, n);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(lcc, dl, n * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(rot, dr, n * 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = fail(nullptr, PF_E_CUDA, "combine: %s", cudaGetErrorString(e));
+  }
+  void* ptrs[] = {dl, dpl, dr, dpr};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  return rc;
+}
+
+}  // extern "C"

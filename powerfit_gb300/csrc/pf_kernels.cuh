@@ -1,0 +1,526 @@
+// Kernels of the exhaustive 6D LCC search (sm_103a).
+//
+// Rotations are processed in pairs.  For a pair (a, b) three complex fields
+// are formed from the rotated template t and mask m (the rotation follows the
+// reference rotate_grid3d, _extensions.c:7-196):
+//     f0 = t_a - i m_a,   f1 = t_b - i m_b,   f2 = m_a^2 - i m_b^2
+// Their spectra F give, after conj(F) * FT(target) or FT(target^2) and an
+// inverse transform (powerfitter.py:349-373 computes the same correlations
+// with six real transforms per rotation):
+//     IFFT(conj(F0) S1) = gcc_a + i ave_a,  IFFT(conj(F1) S1) = gcc_b + i ave_b,
+//     IFFT(conj(F2) S2) = ave2_a + i ave2_b
+// with S1 = FT(target')/N and S2 = FT(target'^2)/N.
+//
+// Three passes per batch of pairs, intermediate spectra laid out
+// buf[pair][field][kx][z][y] (complex float32):
+//   pass 1  per (pair, z, y-tile): rotate/gather, forward x transform, store
+//           transposed so that pass 2 reads contiguous (z, y) planes;
+//   pass 2  per (pair, field, kx): forward y and z transforms of the (z, y)
+//           plane in shared memory, conj product with the target spectrum,
+//           inverse z and y transforms, store in place;
+//   pass 3  per (z, y-tile), looping over the batch's pairs: inverse x
+//           transform, LCC normalisation, running max / argmax kept in
+//           registers for the whole batch.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pf_fft.cuh"
+
+namespace pf {
+
+constexpr int kEmax = 16;          // complex values a thread holds per stage chunk
+constexpr int kThreadsLine = 256;  // pass 1 / pass 3 / target x transform
+constexpr int kThreadsPlane = 512; // pass 2 / target (y, z) transform
+constexpr int kPad = 1;            // shared-memory row padding (complex) for conflict-free access
+
+// 32.32 fixed-point rotation matrix (row-major R, element r_i = round(R_i * 2^32))
+struct RotFixed {
+  long long r[9];
+};
+
+struct Geometry {
+  int nz, ny, nx;
+  int rmax;     // sphere radius of the rotation (min(shape)//2)
+  int reff;     // radius outside which rotated template and mask are known to be zero
+  int nvz;      // number of z planes holding data after rotation (|cz| <= min(rmax, reff))
+  int zlo;      // planes 0..zlo and nz-(nvz-zlo-1)..nz-1 hold data
+};
+
+__device__ __forceinline__ int signed_coord(int i, int n) {
+  // output voxel i of an axis of size n corresponds to offset i (i <= n/2) or i - n;
+  // for even n the voxel n/2 takes the +n/2 offset (written last by the reference loops)
+  return (2 * i <= n) ? i : i - n;
+}
+
+__device__ __forceinline__ int valid_plane(const Geometry& g, int zi) {
+  return (zi <= g.zlo) ? zi : g.nz - g.nvz + zi;
+}
+
+__device__ __forceinline__ int wrap1(int i, int n) {
+  // periodic index; rotation matrices keep i within [-n, 2n), any other
+  // matrix still lands inside the grid
+  if (i >= 0 && i < n) return i;
+  if (i < 0 && i >= -n) return i + n;
+  if (i >= n && i < 2 * n) return i - n;
+  const int r = i % n;
+  return r < 0 ? r + n : r;
+}
+
+// ---------------------------------------------------------------------------
+// Rotation gather (reference rotate_grid3d, _extensions.c:55-180)
+// ---------------------------------------------------------------------------
+// source point q = R^T p in 32.32 fixed point: q_x = r0 x + r3 y + r6 z, etc.
+struct SourcePoint {
+  long long qx, qy, qz;
+};
+
+__device__ __forceinline__ SourcePoint source_point(const RotFixed& R, int cz, int cy, int cx) {
+  SourcePoint s;
+  s.qx = R.r[6] * cz + R.r[3] * cy + R.r[0] * cx;
+  s.qy = R.r[7] * cz + R.r[4] * cy + R.r[1] * cx;
+  s.qz = R.r[8] * cz + R.r[5] * cy + R.r[2] * cx;
+  return s;
+}
+
+// C round() (halves away from zero) of a 32.32 fixed-point value.  Values
+// within 2^-23 of a half are decided in float64 with the reference's operation
+// order (((r6 z) + (r3 y)) + (r0 x), no fused multiply-add), so that the nearest
+// voxel agrees with the float64 reference even when the fixed-point
+// representation of the matrix is 2^-33 away from its float64 value.
+__device__ __forceinline__ int round_fixed(long long q, const double* __restrict__ rd, int c0, int c1, int c2,
+                                           int cz, int cy, int cx) {
+  const long long fl = q >> 32;
+  const unsigned int frac = (unsigned int)(q & 0xffffffffLL);
+  const int dist = (int)(frac - 0x80000000u);
+  if (dist > 512 || dist < -512) return (int)fl + (frac > 0x80000000u ? 1 : 0);
+  double v = __dadd_rn(__dadd_rn(__dmul_rn(rd[c2], (double)cz), __dmul_rn(rd[c1], (double)cy)),
+                       __dmul_rn(rd[c0], (double)cx));
+  return (int)round(v);
+}
+
+struct GatherSrc {
+  const float* __restrict__ tmpl;   // template, float32, C order (z, y, x)
+  const float* __restrict__ mask;   // mask, float32
+};
+
+// trilinear template value and nearest mask value at rotated offset p
+__device__ __forceinline__ void gather_point(const Geometry& g, const GatherSrc& src, const RotFixed& R,
+                                             const double* __restrict__ rd, int cz, int cy, int cx,
+                                             float& t, float& m) {
+  const SourcePoint s = source_point(R, cz, cy, cx);
+  const long long sxy = (long long)g.nx * g.ny;
+  // trilinear (x, then y, then z, as the reference)
+  {
+    const int x0 = (int)(s.qx >> 32), y0 = (int)(s.qy >> 32), z0 = (int)(s.qz >> 32);
+    const float fx = (float)(unsigned int)(s.qx & 0xffffffffLL) * 2.3283064365386963e-10f;
+    const float fy = (float)(unsigned int)(s.qy & 0xffffffffLL) * 2.3283064365386963e-10f;
+    const float fz = (float)(unsigned int)(s.qz & 0xffffffffLL) * 2.3283064365386963e-10f;
+    const int ix0 = wrap1(x0, g.nx), ix1 = wrap1(x0 + 1, g.nx);
+    const long long iy0 = (long long)wrap1(y0, g.ny) * g.nx, iy1 = (long long)wrap1(y0 + 1, g.ny) * g.nx;
+    const long long iz0 = (long long)wrap1(z0, g.nz) * sxy, iz1 = (long long)wrap1(z0 + 1, g.nz) * sxy;
+    const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
+    const float* T = src.tmpl;
+    const float c00 = __ldg(T + iz0 + iy0 + ix0) * gx + __ldg(T + iz0 + iy0 + ix1) * fx;
+    const float c10 = __ldg(T + iz0 + iy1 + ix0) * gx + __ldg(T + iz0 + iy1 + ix1) * fx;
+    const float c01 = __ldg(T + iz1 + iy0 + ix0) * gx + __ldg(T + iz1 + iy0 + ix1) * fx;
+    const float c11 = __ldg(T + iz1 + iy1 + ix0) * gx + __ldg(T + iz1 + iy1 + ix1) * fx;
+    const float c0 = c00 * gy + c10 * fy;
+    const float c1 = c01 * gy + c11 * fy;
+    t = c0 * gz + c1 * fz;
+  }
+  // nearest
+  {
+    const int x0 = round_fixed(s.qx, rd, 0, 3, 6, cz, cy, cx);
+    const int y0 = round_fixed(s.qy, rd, 1, 4, 7, cz, cy, cx);
+    const int z0 = round_fixed(s.qz, rd, 2, 5, 8, cz, cy, cx);
+    m = __ldg(src.mask + (long long)wrap1(z0, g.nz) * sxy + (long long)wrap1(y0, g.ny) * g.nx + wrap1(x0, g.nx));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pass 1: gather + forward x transform, store buf[pair][f][kx][z][y]
+// ---------------------------------------------------------------------------
+struct Pass1Params {
+  Geometry g;
+  AxisPlan px;
+  GatherSrc src;
+  const float2* __restrict__ twx;       // x twiddles (nx entries)
+  const RotFixed* __restrict__ rots;    // fixed-point matrices of this scan
+  const double* __restrict__ rotd;      // float64 matrices (9 per rotation)
+  long long first_rot;                  // rotation index of pair 0, rotation a
+  long long nrot;                       // total rotations of this scan
+  float2* __restrict__ buf;             // intermediate spectra
+  int ty;                               // rows per tile
+};
+
+struct TransposedStore {  // line = f*ty + r  (row y0 + r of field f); idx = kx
+  float2* base;           // buf + pair offset
+  int ty, y0, ny, nz, nx, z;
+  __device__ __forceinline__ void store(int line, int idx, float2 v) const {
+    const int f = line / ty, r = line - f * ty;
+    const int y = y0 + r;
+    if (y < ny) base[(((long long)f * nx + idx) * nz + z) * ny + y] = v;
+  }
+};
+
+__global__ void __launch_bounds__(kThreadsLine) k_pass1(const Pass1Params p) {
+  extern __shared__ float2 sm[];
+  const Geometry& g = p.g;
+  const int X = g.nx;
+  float2* tw = sm;
+  float2* fld = sm + X;                      // [3][ty][X + kPad]
+  const int rs = X + kPad;
+  for (int i = threadIdx.x; i < X; i += blockDim.x) tw[i] = p.twx[i];
+
+  const int z = valid_plane(g, blockIdx.x);
+  const int cz = signed_coord(z, g.nz);
+  const int y0 = blockIdx.y * p.ty;
+  const int pair = blockIdx.z;
+  const long long ra = p.first_rot + 2LL * pair, rb = ra + 1;
+  const bool has_a = ra < p.nrot, has_b = rb < p.nrot;
+  const RotFixed Ra = p.rots[has_a ? ra : 0];
+  const RotFixed Rb = p.rots[has_b ? rb : 0];
+  const double* rda = p.rotd + 9 * (has_a ? ra : 0);
+  const double* rdb = p.rotd + 9 * (has_b ? rb : 0);
+  const int r2 = min(g.rmax, g.reff) * min(g.rmax, g.reff);
+
+  for (int v = threadIdx.x; v < p.ty * X; v += blockDim.x) {
+    const int r = v / X, x = v - r * X;
+    const int y = y0 + r;
+    float ta = 0.f, ma = 0.f, tb = 0.f, mb = 0.f;
+    if (y < g.ny) {
+      const int cy = signed_coord(y, g.ny), cx = signed_coord(x, X);
+      if (cz * cz + cy * cy + cx * cx <= r2) {
+        if (has_a) gather_point(g, p.src, Ra, rda, cz, cy, cx, ta, ma);
+        if (has_b) gather_point(g, p.src, Rb, rdb, cz, cy, cx, tb, mb);
+      }
+    }
+    fld[(0 * p.ty + r) * rs + x] = make_float2(ta, -ma);
+    fld[(1 * p.ty + r) * rs + x] = make_float2(tb, -mb);
+    fld[(2 * p.ty + r) * rs + x] = make_float2(ma * ma, -(mb * mb));
+  }
+  __syncthreads();
+
+  SmemLines lines{fld, rs, 1};
+  TransposedStore out{p.buf + (long long)pair * 3 * g.nx * g.nz * g.ny, p.ty, y0, g.ny, g.nz, g.nx, z};
+  fft_lines<false, kEmax>(p.px, 3 * p.ty, tw, lines, lines, out, true, false);
+}
+
+// ---------------------------------------------------------------------------
+// Pass 2: per (pair, field, kx) plane: y, z forward, product, z, y inverse
+// ---------------------------------------------------------------------------
+struct Pass2Params {
+  Geometry g;
+  AxisPlan py, pz;
+  const float2* __restrict__ twy;
+  const float2* __restrict__ twz;
+  float2* __restrict__ buf;
+  const float2* __restrict__ s1;  // FT(target')/N   layout [kx][kz][ky]
+  const float2* __restrict__ s2;  // FT(target'^2)/N layout [kx][kz][ky]
+  int nfield;                     // fields per pair in buf (3)
+  int mode;                       // 0: correlate (full), 1: forward only -> out
+  float2* __restrict__ out;       // mode 1: spectra, layout [f][kx][kz][ky]
+  float scale;                    // mode 1: multiply spectra by this
+};
+
+struct RowMapLines {  // line l -> data row (valid planes only), element idx along y
+  float2* base;
+  int rs, zlo, shift;
+  __device__ __forceinline__ int row(int l) const { return l <= zlo ? l : l + shift; }
+  __device__ __forceinline__ float2 load(int line, int idx) const { return base[row(line) * rs + idx]; }
+  __device__ __forceinline__ void store(int line, int idx, float2 v) const { base[row(line) * rs + idx] = v; }
+};
+
+struct ProductStore {  // column transforms: line = ky, idx = kz
+  float2* base;
+  int rs;
+  const float2* __restrict__ spec;  // [kz][ky] plane of the target spectrum for this kx
+  int ny;
+  __device__ __forceinline__ void store(int line, int idx, float2 v) const {
+    base[idx * rs + line] = cmulc(v, __ldg(spec + (long long)idx * ny + line));
+  }
+};
+
+__global__ void __launch_bounds__(kThreadsPlane) k_pass2(const Pass2Params p) {
+  extern __shared__ float2 sm[];
+  const Geometry& g = p.g;
+  const int Y = g.ny, Z = g.nz;
+  float2* twy = sm;
+  float2* twz = sm + Y;
+  float2* pl = sm + Y + Z;                      // [Z][Y + kPad]
+  const int rs = Y + kPad;
+  for (int i = threadIdx.x; i < Y; i += blockDim.x) twy[i] = p.twy[i];
+  for (int i = threadIdx.x; i < Z; i += blockDim.x) twz[i] = p.twz[i];
+
+  const int kx = blockIdx.x, f = blockIdx.y, pair = blockIdx.z;
+  const long long plane = (long long)Z * Y;
+  float2* gplane = p.buf + (((long long)pair * p.nfield + f) * g.nx + kx) * plane;
+
+  // load valid rows, zero the rest
+  const int nvz = g.nvz;
+  for (int v = threadIdx.x; v < Z * Y; v += blockDim.x) {
+    const int z = v / Y, y = v - z * Y;
+    const bool valid = (z <= g.zlo) || (z >= Z - (nvz - g.zlo - 1));
+    pl[z * rs + y] = valid ? gplane[(long long)z * Y + y] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+
+  RowMapLines rows{pl, rs, g.zlo, Z - nvz};
+  fft_lines<false, kEmax>(p.py, nvz, twy, rows, rows, rows, true, true);
+  SmemLines cols{pl, 1, rs};
+  if (p.mode == 0) {
+    const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + (long long)kx * plane;
+    ProductStore prod{pl, rs, spec, Y};
+    fft_lines<false, kEmax>(p.pz, Y, twz, cols, cols, prod, true, true);
+    fft_lines<true, kEmax>(p.pz, Y, twz, cols, cols, cols, true, true);
+    SmemLines allrows{pl, rs, 1};
+    fft_lines<true, kEmax>(p.py, Z, twy, allrows, allrows, allrows, true, true);
+    for (int v = threadIdx.x; v < Z * Y; v += blockDim.x) {
+      const int z = v / Y, y = v - z * Y;
+      gplane[(long long)z * Y + y] = pl[z * rs + y];
+    }
+  } else {
+    fft_lines<false, kEmax>(p.pz, Y, twz, cols, cols, cols, true, true);
+    float2* o = p.out + ((long long)f * g.nx + kx) * plane;
+    for (int v = threadIdx.x; v < Z * Y; v += blockDim.x) {
+      const int z = v / Y, y = v - z * Y;
+      o[(long long)z * Y + y] = cscale(pl[z * rs + y], p.scale);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pass 3: inverse x transform, LCC, running max / argmax
+// ---------------------------------------------------------------------------
+struct Pass3Params {
+  Geometry g;
+  AxisPlan px;
+  const float2* __restrict__ twx;
+  const float2* __restrict__ buf;
+  int npairs;                  // pairs in this batch
+  long long first_rot;         // rotation index of pair 0, rotation a (local to the scan)
+  long long nrot;
+  long long rot_offset;        // added to the stored rotation index
+  const unsigned char* __restrict__ lcc_mask;
+  float norm_factor;           // number of mask voxels
+  float* __restrict__ lcc;     // running best (float32)
+  int* __restrict__ rot;       // running argmax
+  int ty;
+  int fp64;                    // 1: variance and LCC in float64
+};
+
+struct GlobalRowsLoad {  // line = f*ty + r, idx = kx: buf[f][kx][z][y0 + r]
+  const float2* base;
+  int ty, y0, ny, nz, nx, z;
+  __device__ __forceinline__ float2 load(int line, int idx) const {
+    const int f = line / ty, r = line - f * ty;
+    const int y = y0 + r;
+    return y < ny ? base[(((long long)f * nx + idx) * nz + z) * ny + y] : make_float2(0.f, 0.f);
+  }
+};
+
+// local variance Nm*ave2 - ave^2 and gcc / sqrt(var), with the subtraction
+// carried in float-float (exact products by FMA, two-sum of the difference)
+__device__ __forceinline__ float lcc_value(float gcc, float ave, float ave2, float nm) {
+  const float p1 = ave2 * nm;
+  const float e1 = fmaf(ave2, nm, -p1);
+  const float p2 = ave * ave;
+  const float e2 = fmaf(ave, ave, -p2);
+  const float s = p1 - p2;
+  const float bb = s - p1;
+  const float err = (p1 - (s - bb)) + (-p2 - bb);
+  const float var = s + ((err + e1) - e2);
+  return gcc / sqrtf(var);
+}
+
+__device__ __forceinline__ float lcc_value64(float gcc, float ave, float ave2, float nm) {
+  const double var = (double)ave2 * (double)nm - (double)ave * (double)ave;
+  return (float)((double)gcc / sqrt(var));
+}
+
+constexpr int kMaxVoxPerThread = 16;
+
+__global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {
+  extern __shared__ float2 sm[];
+  const Geometry& g = p.g;
+  const int X = g.nx;
+  float2* tw = sm;
+  float2* fld = sm + X;                      // [3][ty][X + kPad]
+  const int rs = X + kPad;
+  for (int i = threadIdx.x; i < X; i += blockDim.x) tw[i] = p.twx[i];
+
+  const int z = blockIdx.x;
+  const int y0 = blockIdx.y * p.ty;
+  const int nvox = p.ty * X;
+  const long long zoff = (long long)z * g.ny * X;
+
+  float best[kMaxVoxPerThread];
+  int brot[kMaxVoxPerThread];
+  unsigned int inmask = 0;
+#pragma unroll
+  for (int k = 0; k < kMaxVoxPerThread; ++k) {
+    const int v = threadIdx.x + k * blockDim.x;
+    best[k] = 0.f;
+    brot[k] = 0;
+    if (v < nvox) {
+      const int r = v / X, x = v - r * X;
+      const int y = y0 + r;
+      if (y < g.ny) {
+        const long long gi = zoff + (long long)y * X + x;
+        best[k] = p.lcc[gi];
+        brot[k] = p.rot[gi];
+        if (p.lcc_mask[gi]) inmask |= 1u << k;
+      }
+    }
+  }
+
+  const long long fstride = (long long)g.nx * g.nz * g.ny;
+  for (int pair = 0; pair < p.npairs; ++pair) {
+    GlobalRowsLoad src{p.buf + (long long)pair * 3 * fstride, p.ty, y0, g.ny, g.nz, g.nx, z};
+    SmemLines lines{fld, rs, 1};
+    fft_lines<true, kEmax>(p.px, 3 * p.ty, tw, src, lines, lines, false, true);
+    __syncthreads();
+    const long long ra = p.first_rot + 2LL * pair;
+    const bool has_b = ra + 1 < p.nrot;
+#pragma unroll
+    for (int k = 0; k < kMaxVoxPerThread; ++k) {
+      if (inmask & (1u << k)) {
+        const int v = threadIdx.x + k * blockDim.x;
+        const int r = v / X, x = v - r * X;
+        const float2 f0 = fld[(0 * p.ty + r) * rs + x];
+        const float2 f1 = fld[(1 * p.ty + r) * rs + x];
+        const float2 f2 = fld[(2 * p.ty + r) * rs + x];
+        float la, lb;
+        if (p.fp64) {
+          la = lcc_value64(f0.x, f0.y, f2.x, p.norm_factor);
+          lb = lcc_value64(f1.x, f1.y, f2.y, p.norm_factor);
+        } else {
+          la = lcc_value(f0.x, f0.y, f2.x, p.norm_factor);
+          lb = lcc_value(f1.x, f1.y, f2.y, p.norm_factor);
+        }
+        if (la > best[k]) { best[k] = la; brot[k] = (int)(p.rot_offset + ra); }
+        if (has_b && lb > best[k]) { best[k] = lb; brot[k] = (int)(p.rot_offset + ra + 1); }
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int k = 0; k < kMaxVoxPerThread; ++k) {
+    const int v = threadIdx.x + k * blockDim.x;
+    if (v < nvox) {
+      const int r = v / X, x = v - r * X;
+      const int y = y0 + r;
+      if (y < g.ny) {
+        const long long gi = zoff + (long long)y * X + x;
+        p.lcc[gi] = best[k];
+        p.rot[gi] = brot[k];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Target spectra: x transform of two real fields (target', target'^2)
+// ---------------------------------------------------------------------------
+struct FwdXParams {
+  Geometry g;
+  AxisPlan px;
+  const float2* __restrict__ twx;
+  const float* __restrict__ in0;   // real field 0
+  const float* __restrict__ in1;   // real field 1 (may be null: zeros)
+  int square1;                     // field 1 = in0^2 (in1 ignored)
+  float2* __restrict__ buf;        // [2][kx][z][y]
+  int ty;
+};
+
+__global__ void __launch_bounds__(kThreadsLine) k_fwd_x_real(const FwdXParams p) {
+  extern __shared__ float2 sm[];
+  const Geometry& g = p.g;
+  const int X = g.nx;
+  float2* tw = sm;
+  float2* fld = sm + X;
+  const int rs = X + kPad;
+  for (int i = threadIdx.x; i < X; i += blockDim.x) tw[i] = p.twx[i];
+  const int z = blockIdx.x;
+  const int y0 = blockIdx.y * p.ty;
+  for (int v = threadIdx.x; v < p.ty * X; v += blockDim.x) {
+    const int r = v / X, x = v - r * X;
+    const int y = y0 + r;
+    float a = 0.f, b = 0.f;
+    if (y < g.ny) {
+      const long long gi = ((long long)z * g.ny + y) * X + x;
+      a = p.in0[gi];
+      b = p.square1 ? a * a : (p.in1 ? p.in1[gi] : 0.f);
+    }
+    fld[r * rs + x] = make_float2(a, 0.f);
+    fld[(p.ty + r) * rs + x] = make_float2(b, 0.f);
+  }
+  __syncthreads();
+  SmemLines lines{fld, rs, 1};
+  TransposedStore out{p.buf, p.ty, y0, g.ny, g.nz, g.nx, z};
+  fft_lines<false, kEmax>(p.px, 2 * p.ty, tw, lines, lines, out, true, false);
+}
+
+// ---------------------------------------------------------------------------
+// Unit-level kernels mirroring the reference's native helpers
+// ---------------------------------------------------------------------------
+// rotate_grid3d (_extensions.c:7-196): writes out only inside the sphere
+__global__ void k_rotate_grid(Geometry g, GatherSrc src, RotFixed R, const double* __restrict__ rd, int radius,
+                              int nearest, double* __restrict__ out) {
+  const long long n = (long long)g.nz * g.ny * g.nx;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % g.nx);
+    const int y = (int)((i / g.nx) % g.ny);
+    const int z = (int)(i / ((long long)g.nx * g.ny));
+    // offsets in [-radius, radius] that land on this voxel; the last in loop order wins
+    int cz = -1000000, cy = 0, cx = 0;
+    bool found = false;
+    for (int oz = z - 2 * g.nz; oz <= radius; oz += g.nz) {
+      if (oz < -radius) continue;
+      for (int oy = y - 2 * g.ny; oy <= radius; oy += g.ny) {
+        if (oy < -radius) continue;
+        for (int ox = x - 2 * g.nx; ox <= radius; ox += g.nx) {
+          if (ox < -radius) continue;
+          if (oz * oz + oy * oy + ox * ox <= radius * radius) { cz = oz; cy = oy; cx = ox; found = true; }
+        }
+      }
+    }
+    if (!found) continue;
+    float t, m;
+    gather_point(g, src, R, rd, cz, cy, cx, t, m);
+    out[i] = nearest ? (double)m : (double)t;
+  }
+}
+
+// conj_multiply (_powerfit.pyx:45-53), complex128
+__global__ void k_conj_multiply(const double2* __restrict__ a, const double2* __restrict__ b, double2* __restrict__ o,
+                                long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double2 x = a[i], y = b[i];
+    o[i] = make_double2(x.x * y.x + x.y * y.y, x.x * y.y - x.y * y.x);
+  }
+}
+
+// calc_lcc (_powerfit.pyx:56-72), float64
+__global__ void k_calc_lcc(const double* __restrict__ gcc, const double* __restrict__ ave,
+                           const double* __restrict__ ave2, const unsigned char* __restrict__ mask,
+                           double* __restrict__ lcc, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    if (mask[i]) {
+      const double var = ave2[i] - ave[i] * ave[i];
+      lcc[i] = gcc[i] / sqrt(var);
+    }
+  }
+}
+
+// PowerFitter._combine (powerfitter.py:146-163): strict > merge of rotation shards
+__global__ void k_combine(const float* __restrict__ part_lcc, const int* __restrict__ part_rot, long long rot_add,
+                          float* __restrict__ lcc, int* __restrict__ rot, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float v = part_lcc[i];
+    if (v > lcc[i]) { lcc[i] = v; rot[i] = (int)(part_rot[i] + rot_add); }
+  }
+}
+
+}  // namespace pf

@@ -1,0 +1,234 @@
+"""GPU parity tests: the CUDA path through the C ABI against the reference's
+golden outputs (tests/golden, produced by the real reference) and against the
+oracle restatement run live on the same seeded inputs.
+
+Tolerances (from the search's correctness criterion): best LCC within 1e-4
+absolute; best rotation identical wherever the reference's top-two LCC gap at
+that voxel exceeds 1e-4.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+LCC_TOL = 1e-4
+GAP_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from powerfit_gb300 import _lib
+    return _lib
+
+
+def check_parity(lcc, rot, ref_lcc, ref_rot, ref_second, label=""):
+    ref_lcc = np.asarray(ref_lcc, dtype=np.float64)
+    finite = np.isfinite(ref_lcc)
+    assert np.array_equal(np.isfinite(lcc), finite), label + ": non-finite pattern differs"
+    err = float(np.max(np.abs(lcc[finite] - ref_lcc[finite]))) if finite.any() else 0.0
+    assert err < LCC_TOL, "%s: max |dLCC| = %g" % (label, err)
+    clear = finite & ((ref_lcc - ref_second) > GAP_TOL)
+    bad = int(np.sum(rot[clear] != ref_rot[clear]))
+    assert bad == 0, "%s: %d of %d clear voxels pick a different rotation" % (label, bad, int(clear.sum()))
+    return err
+
+
+def correlator(target, template, mask, rotmats, laplace, flags=0, **tuning):
+    from powerfit_gb300 import CUDACorrelator
+    corr = CUDACorrelator(np.asarray(target, np.float64), laplace=laplace, flags=flags)
+    if tuning:
+        corr.context.set_tuning(**tuning)
+    corr.template = np.asarray(template, np.float64)
+    corr.mask = np.asarray(mask, np.float64)
+    corr.rotations = rotmats
+    corr.scan()
+    return corr
+
+
+# --------------------------------------------------------------------------
+# unit-level mirrors against the reference's own outputs
+# --------------------------------------------------------------------------
+
+def test_rotate_grid3d_golden(lib):
+    d = np.load(os.path.join(GOLD, "rotate_grid3d.npz"))
+    for name in d["names"]:
+        grid = d[name + "_grid"].astype(np.float64)
+        out = np.zeros_like(grid)
+        lib.rotate_grid3d(grid, d[name + "_rotmat"], int(d[name + "_radius"]), out, int(d[name + "_nearest"]))
+        ref = d[name + "_out"]
+        if int(d[name + "_nearest"]):
+            assert np.array_equal(out, ref), name
+        else:
+            assert np.max(np.abs(out - ref)) < 1e-5, (name, np.max(np.abs(out - ref)))
+
+
+def test_rotate_grid3d_preserves_outside(lib):
+    grid = np.random.default_rng(0).random((8, 9, 10))
+    out = np.full_like(grid, 7.0)
+    lib.rotate_grid3d(grid, np.eye(3), 2, out, 1)
+    zz, yy, xx = np.meshgrid(*[np.where(np.arange(n) * 2 <= n, np.arange(n), np.arange(n) - n) for n in grid.shape],
+                             indexing="ij")
+    inside = zz ** 2 + yy ** 2 + xx ** 2 <= 4
+    assert np.all(out[~inside] == 7.0)
+    assert np.allclose(out[inside], grid[inside].astype(np.float32))
+
+
+def test_conj_multiply_and_calc_lcc_golden(lib):
+    d = np.load(os.path.join(GOLD, "lcc_helpers.npz"))
+    out = np.empty_like(d["a"])
+    lib.conj_multiply(d["a"], d["b"], out)
+    assert np.allclose(out, d["conj"], rtol=1e-14, atol=0)
+    lcc = np.full(d["gcc"].shape, -7.0)
+    lib.calc_lcc(d["gcc"], d["ave"], d["ave2"], d["mask"], lcc)
+    ref = d["lcc"]
+    assert np.array_equal(np.isnan(lcc), np.isnan(ref))
+    fin = np.isfinite(ref)
+    assert np.array_equal(np.isinf(lcc), np.isinf(ref))
+    assert np.allclose(lcc[fin], ref[fin], rtol=1e-14)
+
+
+def test_combine_matches_reference_merge(lib):
+    rng = np.random.default_rng(3)
+    parts = [(rng.random(1000).astype(np.float32), rng.integers(0, 50, 1000).astype(np.int32)) for _ in range(3)]
+    parts[1][0][:10] = parts[0][0][:10]        # ties: the earlier shard keeps the voxel
+    from powerfit_gb300 import combine_shards
+    lcc, rot = combine_shards(parts, 50)
+    rlcc, rrot = O.combine([(p[0].astype(np.float64), p[1].astype(np.float64)) for p in parts], 50)
+    assert np.array_equal(lcc, rlcc.astype(np.float32))
+    assert np.array_equal(rot, rrot.astype(np.int32))
+
+
+# --------------------------------------------------------------------------
+# FFT engine
+# --------------------------------------------------------------------------
+
+@pytest.mark.parametrize("shape", [(8, 8, 8), (10, 12, 14), (15, 16, 21), (24, 20, 18), (48, 48, 48),
+                                   (64, 64, 64), (7, 9, 25), (96, 80, 36), (1, 4, 6)])
+def test_fft3d_matches_numpy(lib, shape):
+    a = np.random.default_rng(sum(shape)).standard_normal(shape).astype(np.float32)
+    ctx = lib.Context(shape)
+    out = ctx.fft3d(a)
+    ref = np.fft.fftn(a.astype(np.float64))
+    rel = np.max(np.abs(out - ref)) / np.max(np.abs(ref))
+    assert rel < 2e-6, (shape, rel)
+
+
+# --------------------------------------------------------------------------
+# full scans against the reference's golden outputs
+# --------------------------------------------------------------------------
+
+SCANS = sorted(os.path.basename(p)[5:-4] for p in glob.glob(os.path.join(GOLD, "scan_*.npz")))
+
+
+@pytest.mark.parametrize("name", SCANS)
+def test_scan_golden(name):
+    d = np.load(os.path.join(GOLD, "scan_%s.npz" % name))
+    corr = correlator(d["target"], d["template"], d["mask"], d["rotmats"], bool(d["laplace"]))
+    assert corr.lcc.dtype == np.float32 and corr.rot.dtype == np.int32
+    check_parity(corr.lcc, corr.rot, d["lcc"], d["rot"], d["second"], name)
+
+
+@pytest.mark.parametrize("name", SCANS)
+def test_scan_golden_fp64_normalisation(name):
+    from powerfit_gb300._lib import PF_FLAG_FP64_NORM
+    d = np.load(os.path.join(GOLD, "scan_%s.npz" % name))
+    corr = correlator(d["target"], d["template"], d["mask"], d["rotmats"], bool(d["laplace"]),
+                      flags=PF_FLAG_FP64_NORM)
+    check_parity(corr.lcc, corr.rot, d["lcc"], d["rot"], d["second"], name)
+
+
+# --------------------------------------------------------------------------
+# live oracle comparisons on synthetic maps
+# --------------------------------------------------------------------------
+
+def _synthetic(shape, vs, natoms, res, seed, core_weighted):
+    from powerfit_gb300 import synth
+    c = synth.make_case(shape, vs, natoms, 3, res, 4.0, seed)
+    mask = O.determine_core_indices(c.mask) if core_weighted else c.mask
+    return c.target.astype(np.float64), c.template, mask
+
+
+@pytest.mark.parametrize("laplace,cw", [(False, False), (True, True)])
+def test_scan_oracle_64(laplace, cw):
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    target, template, mask = _synthetic((64, 64, 64), 2.0, 1500, 8.0, 11, cw)
+    rot = quat_to_rotmat(super_fibonacci(300))[::10]   # 30 rotations spread over SO(3)
+    corr = correlator(target, template, mask, rot, laplace)
+    p = O.prepare(target, template, mask, laplace)
+    lcc, rrot, second = O.scan(p, rot, track_second=True)
+    err = check_parity(corr.lcc, corr.rot, lcc, rrot, second, "64^3")
+    print("64^3 laplace=%s cw=%s max|dLCC|=%.2e" % (laplace, cw, err))
+
+
+def test_scan_oracle_128_subset():
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    target, template, mask = _synthetic((128, 128, 128), 1.5, 4000, 6.0, 5, True)
+    rot = quat_to_rotmat(super_fibonacci(4000))[::800]  # 5 rotations
+    corr = correlator(target, template, mask, rot, True)
+    p = O.prepare(target, template, mask, True)
+    lcc, rrot, second = O.scan(p, rot, track_second=True)
+    err = check_parity(corr.lcc, corr.rot, lcc, rrot, second, "128^3")
+    print("128^3 laplace+cw max|dLCC|=%.2e" % err)
+
+
+# --------------------------------------------------------------------------
+# invariances of the batched / pruned implementation (bitwise)
+# --------------------------------------------------------------------------
+
+def test_batching_pruning_and_accumulate_are_exact(lib):
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    from powerfit_gb300._lib import PF_FLAG_ACCUMULATE, PF_FLAG_NO_PRUNE
+    target, template, mask = _synthetic((48, 48, 48), 2.5, 800, 8.0, 3, False)
+    rot = quat_to_rotmat(super_fibonacci(37))            # odd count: last pair half-empty
+    base = correlator(target, template, mask, rot, False)
+    geo = base.context.get_geometry()
+    assert geo["valid_planes"] <= 48
+    ctx = base.context
+    for pairs in (1, 3, 8):
+        ctx.set_tuning(pairs=pairs, rows1=4, rows3=8)
+        lcc, r = ctx.scan(rot)
+        assert np.array_equal(lcc, base.lcc) and np.array_equal(r, base.rot), pairs
+    lcc, r = ctx.scan(rot, flags=PF_FLAG_NO_PRUNE)
+    assert np.array_equal(lcc, base.lcc) and np.array_equal(r, base.rot)
+    # two slices accumulated == one scan
+    ctx.set_rotations(rot)
+    ctx.scan_resident(0, 20)
+    ctx.scan_resident(20, 17, flags=PF_FLAG_ACCUMULATE)
+    lcc, r = ctx.get_results()
+    assert np.array_equal(lcc, base.lcc) and np.array_equal(r, base.rot)
+    # rotation offset is added to the stored index
+    lcc, r = ctx.scan(rot, rot_offset=1000)
+    upd = base.lcc > 0
+    assert np.array_equal(r[upd], base.rot[upd] + 1000)
+
+
+def test_translation_equivariance(lib):
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    target, template, mask = _synthetic((48, 48, 48), 2.5, 800, 8.0, 4, False)
+    rot = quat_to_rotmat(super_fibonacci(8))
+    a = correlator(target, template, mask, rot, False)
+    shift = (5, -7, 11)
+    b = correlator(np.roll(target, shift, axis=(0, 1, 2)), template, mask, rot, False)
+    assert np.max(np.abs(np.roll(a.lcc, shift, axis=(0, 1, 2)) - b.lcc)) < 1e-5
+
+
+# --------------------------------------------------------------------------
+# error contract of the C ABI
+# --------------------------------------------------------------------------
+
+def test_error_contract(lib):
+    with pytest.raises(lib.PowerFitError):
+        lib.Context((11, 16, 16))          # prime factor 11
+    ctx = lib.Context((16, 16, 16))
+    with pytest.raises(lib.PowerFitError):
+        ctx.scan(np.eye(3))                # target/template not set
+    with pytest.raises(lib.PowerFitError):
+        ctx.set_template_mask(np.zeros((16, 16, 16)), np.ones((16, 16, 16)), 0.0, 8)
+    with pytest.raises(lib.PowerFitError):
+        ctx.set_tuning(rows1=100000)
