@@ -1,0 +1,388 @@
+"""Benchmark: rotations/s of the exhaustive 6D LCC search on one GB300.
+
+Workload (default ``lcc128_filtered``): a seeded synthetic 128^3 map at 1.5 A
+per voxel holding 6 copies of a 4,000-atom chain at 6 A resolution, SNR 3;
+Laplace pre-filter and core-weighted LCC; 70,728 rotations (the size of the
+reference's 4.71 degree set; its Karney file is not available on the GPU host,
+so a super-Fibonacci SO(3) set of the same size stands in).
+
+A step scans one eighth of the rotation set (8,841 rotations), accumulating
+the running best, so the default 8 timed steps are one full search.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank scans its own rotations (weak scaling) and
+the per-voxel results are merged on rank 0 after the timed region.
+``--impl reference`` times the reference's CPU correlator path (the oracle
+restatement: numpy.fft, as the reference runs without pyFFTW) on all host
+cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "rotations/s at 128^3 LCC (1 GB300)"
+UNIT = "rotations/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="lcc128_filtered")
+    ap.add_argument("--rotations", type=int, default=0, help="rotation-set size (default: the config's set)")
+    ap.add_argument("--per-step", type=int, default=0, help="rotations per step (default: set size / 8)")
+    ap.add_argument("--cpu-rot-per-core", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--pairs", type=int, default=0)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+def workload(name, nrot_override=0):
+    from powerfit_gb300 import synth
+    from powerfit_gb300.rotations import rotation_set
+    from powerfit_gb300.correlator import determine_core_indices
+    cfg = synth.CONFIGS[name]
+    case = synth.make_config(name, seed=0)
+    mask = determine_core_indices(case.mask) if cfg["core_weighted"] else case.mask
+    rot, desc = rotation_set(cfg["angle"], data_dir=os.environ.get("POWERFIT_ROTATION_DATA") or "/nonexistent")
+    if nrot_override:
+        rot = rot[:nrot_override]
+    return cfg, case.target.astype(np.float64), case.template, mask, rot, desc
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the reference correlator path (oracle restatement) on host cores
+# ---------------------------------------------------------------------------
+
+def make_pool(n):
+    import multiprocessing as mp
+    return mp.get_context("spawn").Pool(n)
+
+
+def cpu_sample(pool, nproc, target, template, mask, rot, laplace, per_core):
+    """Time the reference's _cpu_scan structure on nproc processes over the
+    first nproc*per_core rotations; returns rotations/s."""
+    from oracle import oracle as O
+    sample = rot[: nproc * per_core]
+    t0 = time.perf_counter()
+    O.cpu_scan(target, template, mask, sample, laplace, nproc=nproc, pool=pool)
+    dt = time.perf_counter() - t0
+    return sample.shape[0] / dt, sample.shape[0], dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    pool = make_pool(cores)
+    cfg, target, template, mask, rot, desc = workload(args.config, args.rotations)
+    per_core = args.cpu_rot_per_core
+    for _ in range(max(args.warmup, 0) and 1):
+        cpu_sample(pool, cores, target, template, mask, rot[:cores], cfg["laplace"], 1)
+    vals = []
+    tot_rot, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        v, n, dt = cpu_sample(pool, cores, target, template, mask, rot, cfg["laplace"], per_core)
+        vals.append(v)
+        tot_rot += n
+        tot_t += dt
+    pool.close()
+    value = tot_rot / tot_t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded map, template, mask; %s)" % desc,
+        "config": {"workload": args.config, "grid": list(target.shape), "laplace": cfg["laplace"],
+                   "core_weighted": cfg["core_weighted"], "rotation_set_size": int(rot.shape[0]),
+                   "sample_rotations_per_step": cores * per_core},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "first %d rotations per step (%d per core), _cpu_scan structure, numpy.fft"
+                                   % (cores * per_core, per_core)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
+
+def bytes_per_rotation(n, B):
+    """Compulsory HBM traffic of the three-pass fused pipeline per rotation
+    (F = 3 spectra, complex64 spectra, B rotations sharing target spectra and
+    the running max): 8N + 8H(2F+6) + (16H + 17N)/B, H = n*n*(n/2+1)."""
+    N = n ** 3
+    H = n * n * (n // 2 + 1)
+    return 8 * N + 8 * H * (2 * 3 + 6) + (16 * H + 17 * N) / B
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    cores = os.cpu_count() or 1
+    pool = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        pool = make_pool(cores)          # spawn before any CUDA work
+    torch.cuda.set_device(local_rank)
+    from powerfit_gb300 import _lib
+    from powerfit_gb300.correlator import BaseCorrelator
+
+    cfg, target, template, mask, rot_all, desc = workload(args.config, args.rotations)
+    nset = rot_all.shape[0]
+    per_step = args.per_step or -(-nset // 8)
+    # weak scaling: every rank scans its own rotations (rank r: set shifted by r * per_step)
+    rot_rank = np.roll(rot_all, -rank * per_step, axis=0)
+
+    base = BaseCorrelator(target, laplace=cfg["laplace"])
+    base.template = template
+    base.mask = mask
+    ftarget = base._laplace_filter(base._target) if cfg["laplace"] else base._target
+    shape = target.shape
+    n = shape[0]
+
+    ctx = _lib.Context(shape, local_rank)
+    if args.pairs:
+        ctx.set_tuning(pairs=args.pairs)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_target(ftarget, base._lcc_mask)
+    ctx.set_template_mask(base._template, base._mask, float(base._norm_factor), base._rmax)
+    ctx.set_rotations(rot_rank)
+    pairs, ty1, ty3 = ctx.get_tuning()
+    geo = ctx.get_geometry()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step(k, first):
+        f = (k * per_step) % nset
+        cnt = min(per_step, nset - f)
+        ctx.scan_resident(f, cnt, 0, 0 if first else _lib.PF_FLAG_ACCUMULATE)
+        return cnt
+
+    for w in range(args.warmup):
+        step(w, w == 0)
+    torch.cuda.synchronize()
+
+    # timed region: device-resident inputs, L2 flushed before each step
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    ctx.set_profiling(True)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    done = 0
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        done += step(k, k == 0)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    ms_steps = [a.elapsed_time(b) for a, b in ev]
+    kms, klaunch = ctx.kernel_times()
+    ctx.set_profiling(False)
+    dev_s = sum(ms_steps) / 1e3
+    t = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+    dev_s = float(t.item())
+    value = done * world / dev_s
+
+    # end-to-end through the reference-facing API with host buffers: per step
+    # the whole correlator job for that step's rotations (target and template
+    # upload + spectra, rotations H2D, scan, LCC and rotation volumes D2H)
+    e2e_steps = max(1, min(args.steps, 3))
+    out_lcc = np.empty(shape, np.float32)
+    out_rot = np.empty(shape, np.int32)
+    rot_host = [np.ascontiguousarray(rot_rank[(k * per_step) % nset:(k * per_step) % nset + per_step])
+                for k in range(e2e_steps)]
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    e0 = time.perf_counter()
+    for k in range(e2e_steps):
+        ctx.set_target(ftarget, base._lcc_mask)
+        ctx.set_template_mask(base._template, base._mask, float(base._norm_factor), base._rmax)
+        ctx.set_rotations(rot_host[k])
+        ctx.scan_resident(0, rot_host[k].shape[0], 0, 0)
+        ctx.get_results(out_lcc, out_rot)
+    e2e_s = time.perf_counter() - e0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = sum(r.shape[0] for r in rot_host) * world / float(te.item())
+    N = int(np.prod(shape))
+    h2d = N * 4 + N + N * 4 * 2 + per_step * 9 * 8
+    d2h = N * 8
+
+    # multi-rank: merge per-voxel results on rank 0 (outside the timed region)
+    if world > 1:
+        from powerfit_gb300 import distributed as D
+        lcc_r, rot_r = ctx.get_results()
+        D.gather_and_merge(lcc_r, rot_r, rank_offset=rank * per_step)
+
+    if rank != 0:
+        return 0
+
+    # roofline of the dominant kernel
+    names = ["pass1_rotate_fwdx", "pass2_yz_product", "pass3_invx_lcc"]
+    dom = int(np.argmax(kms))
+    launches = int(klaunch.sum())
+    H = shape[0] * shape[1] * (shape[2] // 2 + 1)
+    nvz = geo["valid_planes"]
+    per_pair = {
+        # pass 1: spectra written (3 complex fields, valid planes only)
+        0: 3 * 8 * N * nvz / shape[0],
+        # pass 2: spectra read (valid planes) + written + target spectrum plane read per field
+        1: 3 * 8 * N * nvz / shape[0] + 3 * 8 * N + 3 * 8 * N,
+        # pass 3: spectra read + (lcc, rot, mask) once per batch
+        2: 3 * 8 * N + 9 * N / pairs,
+    }
+    pairs_per_launch = done / 2.0 / max(klaunch[dom], 1)
+    alg_bytes = per_pair[dom] * pairs_per_launch
+    avg_s = kms[dom] / 1e3 / max(klaunch[dom], 1)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = alg_bytes / avg_s / 1e9
+    pipe_bytes = bytes_per_rotation(n, 2 * pairs)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 FFT / float-float LCC",
+        "data": "synthetic (seeded map, template, mask; %s)" % desc,
+        "config": {"workload": args.config, "grid": list(shape), "voxelspacing": 1.5,
+                   "laplace": cfg["laplace"], "core_weighted": cfg["core_weighted"],
+                   "rotation_set_size": nset, "rotations_per_step": per_step,
+                   "pairs_per_batch": pairs, "rows_pass1": ty1, "rows_pass3": ty3,
+                   "pruned_planes": nvz, "l2": "flushed (256 MiB write) before every timed step",
+                   "full_search_s": nset / (value / world)},
+        "clocks": clk,
+        "wall_s": wall,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "steps": e2e_steps, "note": "per step: target+template upload and spectra, rotations H2D, "
+                                             "scan, lcc+rot D2H"},
+        "gpu_launches": launches,
+        "kernel_ms": {names[i]: float(kms[i]) for i in range(3)},
+        "kernel_launches": {names[i]: int(klaunch[i]) for i in range(3)},
+        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s"},
+        "pipeline_roofline": {"bytes_per_rotation": pipe_bytes, "achieved_gbs": pipe_bytes * value / world / 1e9,
+                              "frac": pipe_bytes * value / world / 1e9 / peak},
+    }
+    if pool is not None:
+        cv, cn, cdt = cpu_sample(pool, cores, target, template, mask, rot_all, cfg["laplace"], args.cpu_rot_per_core)
+        pool.close()
+        line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": "%d rotations (%d per core) of the same workload, %.1f s, "
+                                          "_cpu_scan structure with numpy.fft" % (cn, args.cpu_rot_per_core, cdt)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if args.impl == "ours":
+            torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group(backend)
+    try:
+        if args.impl == "reference":
+            return run_reference(args, rank, world)
+        return run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -74,6 +74,9 @@ int pf_reset_results(pf_ctx *ctx);
 int pf_scan_resident(pf_ctx *ctx, int64_t first, int64_t count, int64_t rot_offset, int flags);
 int pf_get_results(pf_ctx *ctx, float *out_lcc, int32_t *out_rot);
 int pf_synchronize(pf_ctx *ctx);
+/* Launch on the caller's cudaStream_t (NULL: back to the context's own
+ * stream); lets a host framework order the search with its own work. */
+int pf_set_stream(pf_ctx *ctx, void *stream);
 
 /* Tuning: rotation pairs per batch, rows per tile of passes 1 and 3
  * (0 keeps the current value). */

@@ -135,9 +135,9 @@ def lcc_one_rotation(p: Prepared, rotmat, lcc_scan=None):
     rotate_grid3d(p.template, rotmat, p.rmax, rot_t, False)
     rotate_grid3d(p.mask, rotmat, p.rmax, rot_m, True)
     rot_m2 = rot_m * rot_m
-    gcc = irfftn(np.conj(rfftn(rot_t)) * p.ft_target, s=shape)
-    ave = irfftn(np.conj(rfftn(rot_m)) * p.ft_target, s=shape)
-    ave2 = irfftn(np.conj(rfftn(rot_m2)) * p.ft_target2, s=shape)
+    gcc = irfftn(np.conj(rfftn(rot_t)) * p.ft_target, s=shape, axes=(0, 1, 2))
+    ave = irfftn(np.conj(rfftn(rot_m)) * p.ft_target, s=shape, axes=(0, 1, 2))
+    ave2 = irfftn(np.conj(rfftn(rot_m2)) * p.ft_target2, s=shape, axes=(0, 1, 2))
     ave2 *= p.norm_factor
     if lcc_scan is None:
         lcc_scan = np.zeros(shape)

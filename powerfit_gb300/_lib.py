@@ -21,7 +21,7 @@ PF_FLAG_ACCUMULATE = 4
 EXPORTS = [
     "pf_create", "pf_destroy", "pf_last_error", "pf_global_error", "pf_set_target",
     "pf_set_template_mask", "pf_scan", "pf_set_rotations", "pf_reset_results",
-    "pf_scan_resident", "pf_get_results", "pf_synchronize", "pf_set_tuning", "pf_get_tuning",
+    "pf_scan_resident", "pf_get_results", "pf_synchronize", "pf_set_stream", "pf_set_tuning", "pf_get_tuning",
     "pf_get_geometry", "pf_set_profiling", "pf_get_kernel_times", "pf_fft3d",
     "pf_rotate_grid3d", "pf_conj_multiply", "pf_calc_lcc", "pf_combine",
 ]
@@ -77,6 +77,7 @@ def load(path=None):
             "pf_scan_resident": (_i, [_vp, _i64, _i64, _i64, _i]),
             "pf_get_results": (_i, [_vp, _vp, _vp]),
             "pf_synchronize": (_i, [_vp]),
+            "pf_set_stream": (_i, [_vp, _vp]),
             "pf_set_tuning": (_i, [_vp, _i, _i, _i]),
             "pf_get_tuning": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
             "pf_get_geometry": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
@@ -192,6 +193,11 @@ class Context:
 
     def synchronize(self):
         self._call("pf_synchronize")
+
+    def set_stream(self, stream_handle):
+        """Launch on a caller stream (an int cudaStream_t, e.g. torch's
+        ``torch.cuda.current_stream().cuda_stream``); None restores the context's own."""
+        self._call("pf_set_stream", ctypes.c_void_p(stream_handle or None))
 
     def set_tuning(self, pairs=0, rows1=0, rows3=0):
         self._call("pf_set_tuning", int(pairs), int(rows1), int(rows3))

@@ -88,7 +88,8 @@ struct pf_ctx {
   int device = 0;
   int nz = 0, ny = 0, nx = 0;
   long long N = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;     // stream every launch and copy goes to
+  cudaStream_t own_stream = nullptr; // the context's own stream (destroyed with it)
   AxisPlan px{}, py{}, pz{};
   float2 *twx = nullptr, *twy = nullptr, *twz = nullptr;
   float *tmpl = nullptr, *mask = nullptr;
@@ -239,10 +240,6 @@ int timed_launch(pf_ctx* c, int which, Launch&& launch) {
   if (c->profiling) {
     cudaEventRecord(b, c->stream);
     c->pending.push_back({which, {a, b}});
-    if (c->pending.size() > 4096) {
-      cudaEventSynchronize(b);
-      collect_events(c);
-    }
   }
   return PF_OK;
 }
@@ -354,7 +351,9 @@ pf_ctx* pf_create(int nz, int ny, int nx, int device, int* status) {
   c->rmax = std::min(nz, std::min(ny, nx)) / 2;
   choose_tiles(c);
   int rc = PF_OK;
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) rc = PF_E_CUDA;
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+    rc = fail(c, PF_E_CUDA, "stream creation failed");
+  c->stream = c->own_stream;
   const size_t N = (size_t)c->N;
   if (!rc) rc = alloc(c, (void**)&c->twx, nx * sizeof(float2));
   if (!rc) rc = alloc(c, (void**)&c->twy, ny * sizeof(float2));
@@ -393,11 +392,20 @@ int pf_destroy(pf_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   collect_events(c);
   for (auto e : c->ev_pool) cudaEventDestroy(e);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  c->own_stream = nullptr;
   void* ptrs[] = {c->twx, c->twy, c->twz, c->tmpl, c->mask, c->lcc_mask, c->spec, c->lcc, c->rot, c->buf, c->rots, c->rotd};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
+  return PF_OK;
+}
+
+int pf_set_stream(pf_ctx* c, void* stream) {
+  if (!c) return PF_E_ARG;
+  DeviceGuard guard(c->device);
+  PF_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
   return PF_OK;
 }
 

@@ -498,7 +498,8 @@ __global__ void k_conj_multiply(const double2* __restrict__ a, const double2* __
                                 long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const double2 x = a[i], y = b[i];
-    o[i] = make_double2(x.x * y.x + x.y * y.y, x.x * y.y - x.y * y.x);
+    o[i] = make_double2(__dadd_rn(__dmul_rn(x.x, y.x), __dmul_rn(x.y, y.y)),
+                        __dsub_rn(__dmul_rn(x.x, y.y), __dmul_rn(x.y, y.x)));
   }
 }
 
@@ -508,8 +509,10 @@ __global__ void k_calc_lcc(const double* __restrict__ gcc, const double* __restr
                            double* __restrict__ lcc, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     if (mask[i]) {
-      const double var = ave2[i] - ave[i] * ave[i];
-      lcc[i] = gcc[i] / sqrt(var);
+      // separate rounding of the square and the difference, as the reference
+      // computes it (no fused multiply-add): ave2 == ave^2 gives var == 0
+      const double var = __dsub_rn(ave2[i], __dmul_rn(ave[i], ave[i]));
+      lcc[i] = __ddiv_rn(gcc[i], __dsqrt_rn(var));
     }
   }
 }

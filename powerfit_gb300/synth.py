@@ -102,7 +102,8 @@ def make_chain(natoms, rng, step=3.8, min_dist=3.0, rg_target=None, packing=0.2)
     The confining radius is sqrt(5/3) * Rg_target, widened where needed so that
     the 3.0 A exclusion spheres fill at most ``packing`` of the confining ball
     (a sequential walk jams well below random close packing).  On a dead end
-    the walk backs up by a growing number of atoms.
+    the walk backs up by a growing number of atoms; a walk that stays jammed
+    widens the sphere by 2 %.
     """
     if rg_target is None:
         rg_target = 18.0 * (natoms / 1500.0) ** (1.0 / 3.0)
@@ -137,6 +138,10 @@ def make_chain(natoms, rng, step=3.8, min_dist=3.0, rg_target=None, packing=0.2)
         budget -= 1
         if budget < 0:
             raise RuntimeError("chain generation did not converge")
+        if stuck > 24:
+            # persistently jammed: widen the confining sphere a little
+            rconf *= 1.02
+            stuck = 0
         placed = False
         for _ in range(60):
             v = rng.normal(size=3)
