@@ -38,6 +38,7 @@ extern "C" {
 #define PF_FLAG_FP64_NORM 1   /* local variance and LCC in float64 (default: float-float) */
 #define PF_FLAG_NO_PRUNE 2    /* do not skip rotated rows known to be zero */
 #define PF_FLAG_ACCUMULATE 4  /* keep the running best of earlier scans (do not reset) */
+#define PF_FLAG_GENERIC 8     /* use the runtime-planned kernels even where a specialised path exists */
 
 typedef struct pf_ctx pf_ctx;
 

@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(_HERE, "libpowerfit_gb300.so")
 PF_FLAG_FP64_NORM = 1
 PF_FLAG_NO_PRUNE = 2
 PF_FLAG_ACCUMULATE = 4
+PF_FLAG_GENERIC = 8
 
 EXPORTS = [
     "pf_create", "pf_destroy", "pf_last_error", "pf_global_error", "pf_set_target",

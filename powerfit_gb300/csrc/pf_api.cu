@@ -10,9 +10,17 @@
 #include <vector>
 
 #include "../../include/powerfit_gb300.h"
-#include "pf_kernels.cuh"
+#define PF_GENERIC_KERNELS 1  // the runtime-planned kernels are compiled in this unit only
+#include "pf_kernels_ct.cuh"
 
 using namespace pf;
+
+// fast-path kernel tables, one translation unit per cubic grid size
+pf::FastLaunch pf_fast_table_48();
+pf::FastLaunch pf_fast_table_64();
+pf::FastLaunch pf_fast_table_96();
+pf::FastLaunch pf_fast_table_128();
+pf::FastLaunch pf_fast_table_160();
 
 namespace {
 
@@ -108,6 +116,8 @@ struct pf_ctx {
   bool have_target = false, have_template = false;
   int pairs = 1, ty1 = 16, ty3 = 16;
   size_t max_smem = 0;
+  bool fast = false;                 // compile-time-specialised kernels for this grid
+  FastLaunch fl{};
   bool profiling = false;
   double ms[3] = {0, 0, 0};
   long long launches[3] = {0, 0, 0};
@@ -164,8 +174,10 @@ void choose_tiles(pf_ctx* c) {
   int ty = 16;
   while (ty > 1 && ((long long)ty * X > (long long)kMaxVoxPerThread * kThreadsLine || line_smem(X, 3, ty) > 96 * 1024)) ty--;
   c->ty1 = ty;
-  // pass 3: enough tiles to fill the machine (>= 4 per SM on 152 SMs)
+  // pass 3: every voxel of a tile owned by one thread slot; enough tiles to
+  // fill the machine (>= 4 per SM on 152 SMs)
   int ty3 = ty;
+  while (ty3 > 1 && (long long)ty3 * X > (long long)kMaxVoxPerThread * kThreadsLine) ty3--;
   while (ty3 > 2 && (long long)c->nz * ((c->ny + ty3 - 1) / ty3) < 4 * 152) ty3 /= 2;
   c->ty3 = ty3;
   // pairs per batch: intermediate spectra of one batch <= 64 MiB (L2-sized), at least 1, at most 16
@@ -251,7 +263,19 @@ int set_smem_limits(pf_ctx* c) {
   PF_CUDA(c, cudaFuncSetAttribute(k_pass3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(s1, (size_t)48 * 1024)));
   PF_CUDA(c, cudaFuncSetAttribute(k_fwd_x_real, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(s1, (size_t)48 * 1024)));
   PF_CUDA(c, cudaFuncSetAttribute(k_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
+  if (c->fast) PF_CUDA(c, c->fl.set_attrs(std::max(s1, (size_t)48 * 1024), s2));
   return PF_OK;
+}
+
+bool fast_table(int n, FastLaunch* fl) {
+  switch (n) {
+    case 48: *fl = pf_fast_table_48(); return true;
+    case 64: *fl = pf_fast_table_64(); return true;
+    case 96: *fl = pf_fast_table_96(); return true;
+    case 128: *fl = pf_fast_table_128(); return true;
+    case 160: *fl = pf_fast_table_160(); return true;
+    default: return false;
+  }
 }
 
 int upload_double_as_float(pf_ctx* c, float* dst, const double* src, long long n) {
@@ -286,7 +310,8 @@ int forward_two_fields(pf_ctx* c, const float* in0, const float* in1, int square
   p2.out = out;
   p2.scale = scale;
   dim3 g2(c->nx, 2, 1);
-  k_pass2<<<g2, kThreadsPlane, plane_smem(c->ny, c->nz), c->stream>>>(p2);
+  if (c->fast) c->fl.pass2(p2, 0, g2, plane_smem(c->ny, c->nz), c->stream);
+  else k_pass2<<<g2, kThreadsPlane, plane_smem(c->ny, c->nz), c->stream>>>(p2);
   PF_CUDA(c, cudaGetLastError());
   PF_CUDA(c, cudaStreamSynchronize(c->stream));
   return PF_OK;
@@ -349,6 +374,7 @@ pf_ctx* pf_create(int nz, int ny, int nx, int device, int* status) {
     return ret(PF_E_SHAPE);
   }
   c->rmax = std::min(nz, std::min(ny, nx)) / 2;
+  if (nz == ny && ny == nx) c->fast = fast_table(nx, &c->fl);
   choose_tiles(c);
   int rc = PF_OK;
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
@@ -527,12 +553,18 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
   const int P = c->pairs;
   const int ty1 = c->ty1, ty3 = c->ty3;
   const size_t s1 = line_smem(c->nx, 3, ty1), s3 = line_smem(c->nx, 3, ty3), s2 = plane_smem(c->ny, c->nz);
+  const bool fast = c->fast && !(flags & PF_FLAG_GENERIC);
+  const int re = std::min(g.rmax, g.reff);
+  const int re2 = re * re;
   const int64_t end = first + count;
   for (int64_t r0 = first; r0 < end; r0 += 2LL * P) {
     const int npairs = (int)std::min<int64_t>(P, (end - r0 + 1) / 2);
     Pass1Params p1{g, c->px, GatherSrc{c->tmpl, c->mask}, c->twx, c->rots, c->rotd, r0, end, c->buf, ty1};
     dim3 g1(g.nvz, (c->ny + ty1 - 1) / ty1, npairs);
-    rc = timed_launch(c, 0, [&] { k_pass1<<<g1, kThreadsLine, s1, c->stream>>>(p1); });
+    rc = timed_launch(c, 0, [&] {
+      if (fast) c->fl.pass1(p1, re2, g1, s1, c->stream);
+      else k_pass1<<<g1, kThreadsLine, s1, c->stream>>>(p1);
+    });
     if (rc) return rc;
     Pass2Params p2{};
     p2.g = g;
@@ -546,12 +578,18 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     p2.nfield = 3;
     p2.mode = 0;
     dim3 g2(c->nx, 3, npairs);
-    rc = timed_launch(c, 1, [&] { k_pass2<<<g2, kThreadsPlane, s2, c->stream>>>(p2); });
+    rc = timed_launch(c, 1, [&] {
+      if (fast) c->fl.pass2(p2, re2, g2, s2, c->stream);
+      else k_pass2<<<g2, kThreadsPlane, s2, c->stream>>>(p2);
+    });
     if (rc) return rc;
     Pass3Params p3{g, c->px, c->twx, c->buf, npairs, r0, end, rot_offset, c->lcc_mask, c->norm_factor,
                    c->lcc, c->rot, ty3, (flags & PF_FLAG_FP64_NORM) ? 1 : 0};
     dim3 g3(c->nz, (c->ny + ty3 - 1) / ty3, 1);
-    rc = timed_launch(c, 2, [&] { k_pass3<<<g3, kThreadsLine, s3, c->stream>>>(p3); });
+    rc = timed_launch(c, 2, [&] {
+      if (fast) c->fl.pass3(p3, g3, s3, c->stream);
+      else k_pass3<<<g3, kThreadsLine, s3, c->stream>>>(p3);
+    });
     if (rc) return rc;
   }
   return PF_OK;
@@ -591,8 +629,9 @@ int pf_set_tuning(pf_ctx* c, int pairs, int rows1, int rows3) {
     return (long long)ty * c->nx <= (long long)kMaxVoxPerThread * kThreadsLine &&
            line_smem(c->nx, 3, ty) <= std::max(line_smem(c->nx, 3, 16), (size_t)48 * 1024);
   };
-  if (rows1 && !ok_rows(rows1)) return fail(c, PF_E_ARG, "rows_pass1 %d too large for nx %d", rows1, c->nx);
-  if (rows3 && !ok_rows(rows3)) return fail(c, PF_E_ARG, "rows_pass3 %d too large for nx %d", rows3, c->nx);
+  if (rows1 && (!ok_rows(rows1) || rows1 > 32)) return fail(c, PF_E_ARG, "rows_pass1 %d too large for nx %d", rows1, c->nx);
+  if (rows3 && (!ok_rows(rows3) || (long long)rows3 * c->nx > (long long)kMaxVoxPerThread * kThreadsLine))
+    return fail(c, PF_E_ARG, "rows_pass3 %d too large for nx %d", rows3, c->nx);
   if (pairs) {
     DeviceGuard guard(c->device);
     cudaStreamSynchronize(c->stream);

@@ -1,0 +1,164 @@
+// Compile-time-planned shared-memory FFT stages (sm_103a fast path).
+//
+// Same Stockham formulation as pf_fft.cuh, but the transform length, the
+// radix sequence, the thread count and the chunk geometry are template
+// constants: every index computation reduces to shifts and multiplies, the
+// per-thread value arrays stay in registers, and the stages inline into the
+// kernels.  Lines are mapped to threads line-fastest (consecutive threads take
+// consecutive lines), so with an odd row stride every access is free of
+// shared-memory bank conflicts whatever the index pattern of the stage.
+#pragma once
+#include "pf_fft.cuh"
+
+namespace pf {
+
+struct CtPlan {
+  int n;
+  int nst;
+  int r[kMaxStages];
+};
+
+// fewest stages, then the largest smallest radix (same rule as the host planner)
+constexpr int kCtRadices[10] = {16, 12, 10, 8, 7, 6, 5, 4, 3, 2};
+
+struct CtSearch {
+  int best[kMaxStages];
+  int best_n;
+  int best_min;
+  int cur[kMaxStages];
+  int cur_n;
+};
+
+constexpr void ct_rec(CtSearch& s, int rem, int maxr) {
+  if (rem == 1) {
+    if (s.cur_n == 0) return;
+    int mn = 1 << 30;
+    for (int i = 0; i < s.cur_n; ++i) mn = s.cur[i] < mn ? s.cur[i] : mn;
+    if (s.best_n == 0 || s.cur_n < s.best_n || (s.cur_n == s.best_n && mn > s.best_min)) {
+      for (int i = 0; i < s.cur_n; ++i) s.best[i] = s.cur[i];
+      s.best_n = s.cur_n;
+      s.best_min = mn;
+    }
+    return;
+  }
+  if (s.best_n != 0 && s.cur_n + 1 > s.best_n) return;
+  if (s.cur_n >= kMaxStages) return;
+  for (int k = 0; k < 10; ++k) {
+    const int r = kCtRadices[k];
+    if (r > maxr || rem % r) continue;
+    s.cur[s.cur_n++] = r;
+    ct_rec(s, rem / r, r);
+    s.cur_n--;
+  }
+}
+
+constexpr CtPlan ct_plan(int n) {
+  CtPlan p{};
+  p.n = n;
+  if (n == 1) {
+    p.nst = 1;
+    p.r[0] = 1;
+    return p;
+  }
+  CtSearch s{};
+  ct_rec(s, n, 16);
+  p.nst = s.best_n;
+  for (int i = 0; i < s.best_n; ++i) p.r[i] = s.best[i];
+  return p;
+}
+
+constexpr int ct_stage_ns(int n, int stage) {
+  CtPlan p = ct_plan(n);
+  int ns = 1;
+  for (int i = 0; i < stage; ++i) ns *= p.r[i];
+  return ns;
+}
+
+constexpr int ct_floor_pow2(int v) {
+  int p = 1;
+  while (p * 2 <= v) p *= 2;
+  return p;
+}
+
+// One radix-R stage over `nlines` lines of length L.  Lines are processed in
+// chunks of C (a power of two) lines; every item (line, butterfly) of a chunk
+// is loaded into registers before any is stored, so src and dst may alias.
+template <int R, bool INV, int L, int NS, int NT, int EMAX, class Src, class Dst>
+__device__ __forceinline__ void ct_stage(int nlines, const float2* __restrict__ tw, const Src& src, const Dst& dst,
+                                         bool alias) {
+  constexpr int NB = L / R;
+  constexpr int KMAX = (EMAX / R) > 0 ? (EMAX / R) : 1;
+  constexpr int C0 = (NT * KMAX) / NB;
+  constexpr int C = ct_floor_pow2(C0 > 0 ? C0 : 1);
+  constexpr int K = (C * NB + NT - 1) / NT;          // items per thread per chunk
+  constexpr int TWMUL = L / (NS * R);
+  for (int l0 = 0; l0 < nlines; l0 += C) {
+    float2 v[K][R];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int it = threadIdx.x + k * NT;
+      const int line = l0 + (it & (C - 1));
+      const int j = it / C;                          // C is a power of two
+      if (j < NB && line < nlines) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[k][r] = src.load(line, j + r * NB);
+        if constexpr (NS > 1) {
+          const int jm = (j % NS) * TWMUL;
+#pragma unroll
+          for (int r = 1; r < R; ++r) {
+            float2 w = tw[r * jm];
+            if (INV) w.y = -w.y;
+            v[k][r] = cmul(v[k][r], w);
+          }
+        }
+        DFT<R, INV>::run(v[k]);
+      }
+    }
+    if (alias) __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int it = threadIdx.x + k * NT;
+      const int line = l0 + (it & (C - 1));
+      const int j = it / C;
+      if (j < NB && line < nlines) {
+        const int base = (j / NS) * NS * R + (j % NS);
+#pragma unroll
+        for (int r = 0; r < R; ++r) dst.store(line, base + r * NS, v[k][r]);
+      }
+    }
+    if (alias) __syncthreads();
+  }
+}
+
+template <int L, bool INV, int NT, int EMAX, int S, class Src, class Mid, class Dst>
+__device__ __forceinline__ void ct_lines_from(int nlines, const float2* __restrict__ tw, const Src& src,
+                                              const Mid& mid, const Dst& dst, bool src_alias, bool dst_alias) {
+  constexpr CtPlan P = ct_plan(L);
+  if constexpr (S < P.nst) {
+    constexpr int R = P.r[S];
+    constexpr int NS = ct_stage_ns(L, S);
+    if constexpr (P.nst == 1) {
+      ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, src, dst, src_alias || dst_alias);
+    } else if constexpr (S == 0) {
+      ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, src, mid, src_alias);
+      __syncthreads();
+    } else if constexpr (S == P.nst - 1) {
+      ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, mid, dst, dst_alias);
+    } else {
+      ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, mid, mid, true);
+      __syncthreads();
+    }
+    ct_lines_from<L, INV, NT, EMAX, S + 1>(nlines, tw, src, mid, dst, src_alias, dst_alias);
+  }
+}
+
+// Full length-L transform of `nlines` lines: first stage reads `src`, last
+// writes `dst`, the others work in `mid` (shared memory).  Ends with a barrier.
+template <int L, bool INV, int NT, int EMAX, class Src, class Mid, class Dst>
+__device__ __forceinline__ void ct_lines(int nlines, const float2* __restrict__ tw, const Src& src, const Mid& mid,
+                                         const Dst& dst, bool src_alias, bool dst_alias) {
+  ct_lines_from<L, INV, NT, EMAX, 0>(nlines, tw, src, mid, dst, src_alias, dst_alias);
+  __syncthreads();
+}
+
+}  // namespace pf

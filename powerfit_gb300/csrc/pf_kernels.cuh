@@ -164,6 +164,7 @@ struct TransposedStore {  // line = f*ty + r  (row y0 + r of field f); idx = kx
   }
 };
 
+#ifdef PF_GENERIC_KERNELS
 __global__ void __launch_bounds__(kThreadsLine) k_pass1(const Pass1Params p) {
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
@@ -207,6 +208,8 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass1(const Pass1Params p) {
   fft_lines<false, kEmax>(p.px, 3 * p.ty, tw, lines, lines, out, true, false);
 }
 
+#endif  // PF_GENERIC_KERNELS
+
 // ---------------------------------------------------------------------------
 // Pass 2: per (pair, field, kx) plane: y, z forward, product, z, y inverse
 // ---------------------------------------------------------------------------
@@ -242,6 +245,7 @@ struct ProductStore {  // column transforms: line = ky, idx = kz
   }
 };
 
+#ifdef PF_GENERIC_KERNELS
 __global__ void __launch_bounds__(kThreadsPlane) k_pass2(const Pass2Params p) {
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
@@ -289,6 +293,8 @@ __global__ void __launch_bounds__(kThreadsPlane) k_pass2(const Pass2Params p) {
     }
   }
 }
+
+#endif  // PF_GENERIC_KERNELS
 
 // ---------------------------------------------------------------------------
 // Pass 3: inverse x transform, LCC, running max / argmax
@@ -339,8 +345,9 @@ __device__ __forceinline__ float lcc_value64(float gcc, float ave, float ave2, f
   return (float)((double)gcc / sqrt(var));
 }
 
-constexpr int kMaxVoxPerThread = 16;
+constexpr int kMaxVoxPerThread = 8;   // pass 3: voxels per thread (tile rows * nx <= 8 * 256)
 
+#ifdef PF_GENERIC_KERNELS
 __global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
@@ -420,6 +427,8 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {
   }
 }
 
+#endif  // PF_GENERIC_KERNELS
+
 // ---------------------------------------------------------------------------
 // Target spectra: x transform of two real fields (target', target'^2)
 // ---------------------------------------------------------------------------
@@ -434,6 +443,7 @@ struct FwdXParams {
   int ty;
 };
 
+#ifdef PF_GENERIC_KERNELS
 __global__ void __launch_bounds__(kThreadsLine) k_fwd_x_real(const FwdXParams p) {
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
@@ -462,9 +472,12 @@ __global__ void __launch_bounds__(kThreadsLine) k_fwd_x_real(const FwdXParams p)
   fft_lines<false, kEmax>(p.px, 2 * p.ty, tw, lines, lines, out, true, false);
 }
 
+#endif  // PF_GENERIC_KERNELS
+
 // ---------------------------------------------------------------------------
 // Unit-level kernels mirroring the reference's native helpers
 // ---------------------------------------------------------------------------
+#ifdef PF_GENERIC_KERNELS
 // rotate_grid3d (_extensions.c:7-196): writes out only inside the sphere
 __global__ void k_rotate_grid(Geometry g, GatherSrc src, RotFixed R, const double* __restrict__ rd, int radius,
                               int nearest, double* __restrict__ out) {
@@ -525,5 +538,7 @@ __global__ void k_combine(const float* __restrict__ part_lcc, const int* __restr
     if (v > lcc[i]) { lcc[i] = v; rot[i] = (int)(part_rot[i] + rot_add); }
   }
 }
+
+#endif  // PF_GENERIC_KERNELS
 
 }  // namespace pf

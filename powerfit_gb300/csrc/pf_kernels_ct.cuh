@@ -1,0 +1,260 @@
+// Fast-path kernels for grids whose edges are compile-time constants.
+//
+// Same three passes and buffer layout as pf_kernels.cuh, plus pruning of the
+// (z, y) rows that the rotation cannot reach: with re = min(rmax, reff), a
+// row whose offsets satisfy cz^2 + cy^2 > re^2 holds only zeros for every
+// rotation, so pass 1 neither transforms nor stores it and pass 2 reads zeros
+// for it without touching memory.
+#pragma once
+#include "pf_fft_ct.cuh"
+#include "pf_kernels.cuh"
+
+namespace pf {
+
+__device__ __forceinline__ bool row_in_disk(const Geometry& g, int cz, int cy, int re2) {
+  return cz * cz + cy * cy <= re2;
+}
+
+// ---------------------------------------------------------------------------
+// Pass 1 (fast): gather + forward x transform of rows inside the disk
+// ---------------------------------------------------------------------------
+template <int X>
+struct DiskTransposedStore {  // line = f*ty + r; idx = kx; rows outside the disk are skipped
+  float2* base;
+  int ty, y0, ny, nz, z;
+  unsigned int rowmask;        // bit r set: row y0 + r is inside the disk
+  __device__ __forceinline__ void store(int line, int idx, float2 v) const {
+    const int f = line / ty, r = line - f * ty;
+    if ((rowmask >> r) & 1u) base[(((long long)f * X + idx) * nz + z) * ny + (y0 + r)] = v;
+  }
+};
+
+template <int X>
+__global__ void __launch_bounds__(kThreadsLine) k_pass1_ct(const Pass1Params p, const int re2) {
+  extern __shared__ float2 sm[];
+  const Geometry& g = p.g;
+  constexpr int rs = X + kPad;
+  float2* tw = sm;
+  float2* fld = sm + X;
+  const int z = valid_plane(g, blockIdx.x);
+  const int cz = signed_coord(z, g.nz);
+  const int y0 = blockIdx.y * p.ty;
+  unsigned int rowmask = 0;
+  for (int r = 0; r < p.ty; ++r) {
+    const int y = y0 + r;
+    if (y < g.ny && row_in_disk(g, cz, signed_coord(y, g.ny), re2)) rowmask |= 1u << r;
+  }
+  if (rowmask == 0) return;                 // whole tile outside the disk (uniform per block)
+  for (int i = threadIdx.x; i < X; i += kThreadsLine) tw[i] = p.twx[i];
+
+  const int pair = blockIdx.z;
+  const long long ra = p.first_rot + 2LL * pair, rb = ra + 1;
+  const bool has_a = ra < p.nrot, has_b = rb < p.nrot;
+  const RotFixed Ra = p.rots[has_a ? ra : 0];
+  const RotFixed Rb = p.rots[has_b ? rb : 0];
+  const double* rda = p.rotd + 9 * (has_a ? ra : 0);
+  const double* rdb = p.rotd + 9 * (has_b ? rb : 0);
+  const int r2 = min(g.rmax, g.reff) * min(g.rmax, g.reff);
+
+  for (int v = threadIdx.x; v < p.ty * X; v += kThreadsLine) {
+    const int r = v / X, x = v - r * X;
+    float ta = 0.f, ma = 0.f, tb = 0.f, mb = 0.f;
+    if ((rowmask >> r) & 1u) {
+      const int cy = signed_coord(y0 + r, g.ny), cx = signed_coord(x, X);
+      if (cz * cz + cy * cy + cx * cx <= r2) {
+        if (has_a) gather_point(g, p.src, Ra, rda, cz, cy, cx, ta, ma);
+        if (has_b) gather_point(g, p.src, Rb, rdb, cz, cy, cx, tb, mb);
+      }
+    }
+    fld[(0 * p.ty + r) * rs + x] = make_float2(ta, -ma);
+    fld[(1 * p.ty + r) * rs + x] = make_float2(tb, -mb);
+    fld[(2 * p.ty + r) * rs + x] = make_float2(ma * ma, -(mb * mb));
+  }
+  __syncthreads();
+  SmemLines lines{fld, rs, 1};
+  DiskTransposedStore<X> out{p.buf + (long long)pair * 3 * X * g.nz * g.ny, p.ty, y0, g.ny, g.nz, z, rowmask};
+  ct_lines<X, false, kThreadsLine, kEmax>(3 * p.ty, tw, lines, lines, out, true, false);
+}
+
+// ---------------------------------------------------------------------------
+// Pass 2 (fast): (z, y) plane per (pair, field, kx)
+// ---------------------------------------------------------------------------
+template <int Y, int Z>
+__global__ void __launch_bounds__(kThreadsPlane) k_pass2_ct(const Pass2Params p, const int re2) {
+  extern __shared__ float2 sm[];
+  const Geometry& g = p.g;
+  constexpr int rs = Y + kPad;
+  float2* twy = sm;
+  float2* twz = sm + Y;
+  float2* pl = sm + Y + Z;
+  for (int i = threadIdx.x; i < Y; i += kThreadsPlane) twy[i] = p.twy[i];
+  for (int i = threadIdx.x; i < Z; i += kThreadsPlane) twz[i] = p.twz[i];
+
+  const int kx = blockIdx.x, f = blockIdx.y, pair = blockIdx.z;
+  constexpr long long plane = (long long)Z * Y;
+  float2* gplane = p.buf + (((long long)pair * p.nfield + f) * g.nx + kx) * plane;
+  const int nvz = g.nvz;
+  const int lo_end = g.zlo, hi_start = Z - (nvz - g.zlo - 1);
+
+  if (p.mode == 0) {
+    for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlane) {
+      const int z = v / Y, y = v - z * Y;
+      const bool valid = (z <= lo_end || z >= hi_start) &&
+                         row_in_disk(g, signed_coord(z, Z), signed_coord(y, Y), re2);
+      pl[z * rs + y] = valid ? gplane[(long long)z * Y + y] : make_float2(0.f, 0.f);
+    }
+  } else {
+    for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlane) {
+      const int z = v / Y, y = v - z * Y;
+      pl[z * rs + y] = gplane[(long long)z * Y + y];
+    }
+  }
+  __syncthreads();
+
+  RowMapLines rows{pl, rs, g.zlo, Z - nvz};
+  ct_lines<Y, false, kThreadsPlane, kEmax>(nvz, twy, rows, rows, rows, true, true);
+  SmemLines cols{pl, 1, rs};
+  if (p.mode == 0) {
+    const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + (long long)kx * plane;
+    ProductStore prod{pl, rs, spec, Y};
+    ct_lines<Z, false, kThreadsPlane, kEmax>(Y, twz, cols, cols, prod, true, true);
+    ct_lines<Z, true, kThreadsPlane, kEmax>(Y, twz, cols, cols, cols, true, true);
+    SmemLines allrows{pl, rs, 1};
+    ct_lines<Y, true, kThreadsPlane, kEmax>(Z, twy, allrows, allrows, allrows, true, true);
+    for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlane) {
+      const int z = v / Y, y = v - z * Y;
+      gplane[(long long)z * Y + y] = pl[z * rs + y];
+    }
+  } else {
+    ct_lines<Z, false, kThreadsPlane, kEmax>(Y, twz, cols, cols, cols, true, true);
+    float2* o = p.out + ((long long)f * g.nx + kx) * plane;
+    for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlane) {
+      const int z = v / Y, y = v - z * Y;
+      o[(long long)z * Y + y] = cscale(pl[z * rs + y], p.scale);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pass 3 (fast): inverse x transform, LCC, running max / argmax
+// ---------------------------------------------------------------------------
+template <int X>
+struct GlobalRowsLoadCt {  // line = f*ty + r, idx = kx: buf[f][kx][z][y0 + r]
+  const float2* base;
+  int ty, y0, ny, nz, z;
+  __device__ __forceinline__ float2 load(int line, int idx) const {
+    const int f = line / ty, r = line - f * ty;
+    const int y = y0 + r;
+    return y < ny ? base[(((long long)f * X + idx) * nz + z) * ny + y] : make_float2(0.f, 0.f);
+  }
+};
+
+template <int X>
+__global__ void __launch_bounds__(kThreadsLine, 2) k_pass3_ct(const Pass3Params p) {
+  extern __shared__ float2 sm[];
+  const Geometry& g = p.g;
+  constexpr int rs = X + kPad;
+  float2* tw = sm;
+  float2* fld = sm + X;
+  for (int i = threadIdx.x; i < X; i += kThreadsLine) tw[i] = p.twx[i];
+
+  const int z = blockIdx.x;
+  const int y0 = blockIdx.y * p.ty;
+  const int nvox = p.ty * X;
+  const long long zoff = (long long)z * g.ny * X;
+
+  float best[kMaxVoxPerThread];
+  int brot[kMaxVoxPerThread];
+  unsigned int inmask = 0;
+#pragma unroll
+  for (int k = 0; k < kMaxVoxPerThread; ++k) {
+    const int v = threadIdx.x + k * kThreadsLine;
+    best[k] = 0.f;
+    brot[k] = 0;
+    if (v < nvox) {
+      const int r = v / X, x = v - r * X;
+      const int y = y0 + r;
+      if (y < g.ny) {
+        const long long gi = zoff + (long long)y * X + x;
+        best[k] = p.lcc[gi];
+        brot[k] = p.rot[gi];
+        if (p.lcc_mask[gi]) inmask |= 1u << k;
+      }
+    }
+  }
+
+  const long long fstride = (long long)X * g.nz * g.ny;
+  for (int pair = 0; pair < p.npairs; ++pair) {
+    GlobalRowsLoadCt<X> src{p.buf + (long long)pair * 3 * fstride, p.ty, y0, g.ny, g.nz, z};
+    SmemLines lines{fld, rs, 1};
+    ct_lines<X, true, kThreadsLine, kEmax>(3 * p.ty, tw, src, lines, lines, false, true);
+    const long long ra = p.first_rot + 2LL * pair;
+    const bool has_b = ra + 1 < p.nrot;
+#pragma unroll
+    for (int k = 0; k < kMaxVoxPerThread; ++k) {
+      if (inmask & (1u << k)) {
+        const int v = threadIdx.x + k * kThreadsLine;
+        const int r = v / X, x = v - r * X;
+        const float2 f0 = fld[(0 * p.ty + r) * rs + x];
+        const float2 f1 = fld[(1 * p.ty + r) * rs + x];
+        const float2 f2 = fld[(2 * p.ty + r) * rs + x];
+        float la, lb;
+        if (p.fp64) {
+          la = lcc_value64(f0.x, f0.y, f2.x, p.norm_factor);
+          lb = lcc_value64(f1.x, f1.y, f2.y, p.norm_factor);
+        } else {
+          la = lcc_value(f0.x, f0.y, f2.x, p.norm_factor);
+          lb = lcc_value(f1.x, f1.y, f2.y, p.norm_factor);
+        }
+        if (la > best[k]) { best[k] = la; brot[k] = (int)(p.rot_offset + ra); }
+        if (has_b && lb > best[k]) { best[k] = lb; brot[k] = (int)(p.rot_offset + ra + 1); }
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int k = 0; k < kMaxVoxPerThread; ++k) {
+    const int v = threadIdx.x + k * kThreadsLine;
+    if (v < nvox) {
+      const int r = v / X, x = v - r * X;
+      const int y = y0 + r;
+      if (y < g.ny) {
+        const long long gi = zoff + (long long)y * X + x;
+        p.lcc[gi] = best[k];
+        p.rot[gi] = brot[k];
+      }
+    }
+  }
+}
+
+// Launchers instantiated once per fast size (pf_fast_<n>.cu)
+struct FastLaunch {
+  void (*pass1)(const Pass1Params&, int re2, dim3 grid, size_t smem, cudaStream_t s);
+  void (*pass2)(const Pass2Params&, int re2, dim3 grid, size_t smem, cudaStream_t s);
+  void (*pass3)(const Pass3Params&, dim3 grid, size_t smem, cudaStream_t s);
+  cudaError_t (*set_attrs)(size_t smem_line, size_t smem_plane);
+};
+
+template <int N>
+struct FastSize {
+  static void pass1(const Pass1Params& p, int re2, dim3 grid, size_t smem, cudaStream_t s) {
+    k_pass1_ct<N><<<grid, kThreadsLine, smem, s>>>(p, re2);
+  }
+  static void pass2(const Pass2Params& p, int re2, dim3 grid, size_t smem, cudaStream_t s) {
+    k_pass2_ct<N, N><<<grid, kThreadsPlane, smem, s>>>(p, re2);
+  }
+  static void pass3(const Pass3Params& p, dim3 grid, size_t smem, cudaStream_t s) {
+    k_pass3_ct<N><<<grid, kThreadsLine, smem, s>>>(p);
+  }
+  static cudaError_t set_attrs(size_t smem_line, size_t smem_plane) {
+    cudaError_t e = cudaFuncSetAttribute(k_pass1_ct<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_line);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_pass3_ct<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_line);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_pass2_ct<N, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_plane);
+    return e;
+  }
+  static FastLaunch table() { return FastLaunch{&pass1, &pass2, &pass3, &set_attrs}; }
+};
+
+}  // namespace pf

@@ -232,3 +232,19 @@ def test_error_contract(lib):
         ctx.set_template_mask(np.zeros((16, 16, 16)), np.ones((16, 16, 16)), 0.0, 8)
     with pytest.raises(lib.PowerFitError):
         ctx.set_tuning(rows1=100000)
+
+
+@pytest.mark.parametrize("n", [48, 64, 96, 128, 160])
+def test_fast_path_equals_generic(lib, n):
+    """The compile-time-specialised kernels (cubic grids) give the same result
+    as the runtime-planned ones."""
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    from powerfit_gb300._lib import PF_FLAG_GENERIC
+    from powerfit_gb300 import synth
+    c = synth.make_case((n, n, n), 192.0 / n, 1200, 2, 6.0, 4.0, 13)
+    rot = quat_to_rotmat(super_fibonacci(9))
+    corr = correlator(c.target.astype(np.float64), c.template, O.determine_core_indices(c.mask), rot, True)
+    lg, rg = corr.context.scan(rot, flags=PF_FLAG_GENERIC)
+    assert np.max(np.abs(corr.lcc - lg)) <= 1e-6
+    upd = np.abs(corr.lcc - lg) == 0
+    assert np.mean(corr.rot[upd] == rg[upd]) == 1.0
