@@ -224,6 +224,11 @@ def run_ours(args, rank, world, local_rank):
     ctx.set_target(ftarget, base._lcc_mask)
     ctx.set_template_mask(base._template, base._mask, float(base._norm_factor), base._rmax)
     ctx.set_rotations(rot_rank)
+    if args.pairs:
+        tuned = {"pairs": args.pairs, "source": "--pairs"}
+    else:
+        tuned = ctx.autotune(512)
+        tuned["source"] = "autotuner (512-rotation trials)"
     pairs, ty1, ty3 = ctx.get_tuning()
     geo = ctx.get_geometry()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -234,32 +239,38 @@ def run_ours(args, rank, world, local_rank):
         ctx.scan_resident(f, cnt, 0, 0 if first else _lib.PF_FLAG_ACCUMULATE)
         return cnt
 
+    def timed(profile):
+        ctx.set_profiling(profile)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        done = 0
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            done += step(k, k == 0)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        kms, kl = ctx.kernel_times()
+        ctx.set_profiling(False)
+        return done, sum(a.elapsed_time(b) for a, b in ev) / 1e3, wall, kms, kl
+
     for w in range(args.warmup):
         step(w, w == 0)
     torch.cuda.synchronize()
 
-    # timed region: device-resident inputs, L2 flushed before each step
+    # timed region: device-resident inputs, L2 flushed before each step, no
+    # per-kernel instrumentation
     clocks = ClockSampler(local_rank)
     clocks.start()
-    ctx.set_profiling(True)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    done = 0
-    for k in range(args.steps):
-        flush.zero_()
-        ev[k][0].record(stream)
-        done += step(k, k == 0)
-        ev[k][1].record(stream)
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
+    done, dev_s, wall, _, _ = timed(False)
     clk = clocks.stop()
-    ms_steps = [a.elapsed_time(b) for a, b in ev]
-    kms, klaunch = ctx.kernel_times()
-    ctx.set_profiling(False)
-    dev_s = sum(ms_steps) / 1e3
+    # the same steps again with CUDA events around every kernel launch (the
+    # per-kernel durations for the roofline)
+    _, prof_s, _, kms, klaunch = timed(True)
     t = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -303,23 +314,26 @@ def run_ours(args, rank, world, local_rank):
     if rank != 0:
         return 0
 
-    # roofline of the dominant kernel
+    # roofline of the dominant kernel: algorithmic bytes per launch / average launch time
     names = ["pass1_rotate_fwdx", "pass2_yz_product", "pass3_invx_lcc"]
     dom = int(np.argmax(kms))
     launches = int(klaunch.sum())
-    H = shape[0] * shape[1] * (shape[2] // 2 + 1)
-    nvz = geo["valid_planes"]
+    nz, ny, nx = shape
+    re = min(geo["rmax"], geo["reff"])
+    cz = np.where(2 * np.arange(nz) <= nz, np.arange(nz), np.arange(nz) - nz)
+    cy = np.where(2 * np.arange(ny) <= ny, np.arange(ny), np.arange(ny) - ny)
+    disk = int(np.sum(cz[:, None] ** 2 + cy[None, :] ** 2 <= re * re))   # (z, y) rows the rotation reaches
+    pairs_per_launch = done / 2.0 / max(int(klaunch[dom]), 1)
     per_pair = {
-        # pass 1: spectra written (3 complex fields, valid planes only)
-        0: 3 * 8 * N * nvz / shape[0],
-        # pass 2: spectra read (valid planes) + written + target spectrum plane read per field
-        1: 3 * 8 * N * nvz / shape[0] + 3 * 8 * N + 3 * 8 * N,
-        # pass 3: spectra read + (lcc, rot, mask) once per batch
-        2: 3 * 8 * N + 9 * N / pairs,
+        # template + mask read once (L2-resident), 3 spectra rows written for the disk rows
+        0: 8 * N / pairs_per_launch + 3 * 8 * disk * nx,
+        # per (field, kx) plane: disk entries read, full plane written, target spectrum plane read
+        1: 3 * nx * 8 * (disk + 2 * nz * ny),
+        # 3 spectra read; lcc + rot read and written and the lcc mask read once per launch
+        2: 3 * 8 * N + (17 * N) / pairs_per_launch,
     }
-    pairs_per_launch = done / 2.0 / max(klaunch[dom], 1)
     alg_bytes = per_pair[dom] * pairs_per_launch
-    avg_s = kms[dom] / 1e3 / max(klaunch[dom], 1)
+    avg_s = kms[dom] / 1e3 / max(int(klaunch[dom]), 1)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -328,6 +342,7 @@ def run_ours(args, rank, world, local_rank):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = alg_bytes / avg_s / 1e9
     pipe_bytes = bytes_per_rotation(n, 2 * pairs)
+    pruned_bytes = sum(per_pair.values()) / 2.0
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
@@ -336,8 +351,9 @@ def run_ours(args, rank, world, local_rank):
         "config": {"workload": args.config, "grid": list(shape), "voxelspacing": 1.5,
                    "laplace": cfg["laplace"], "core_weighted": cfg["core_weighted"],
                    "rotation_set_size": nset, "rotations_per_step": per_step,
-                   "pairs_per_batch": pairs, "rows_pass1": ty1, "rows_pass3": ty3,
-                   "pruned_planes": nvz, "l2": "flushed (256 MiB write) before every timed step",
+                   "pairs_per_batch": pairs, "rows_pass1": ty1, "rows_pass3": ty3, "tuning": tuned,
+                   "reach_radius": re, "planes": geo["valid_planes"], "disk_rows": disk,
+                   "l2": "flushed (256 MiB write) before every timed step",
                    "full_search_s": nset / (value / world)},
         "clocks": clk,
         "wall_s": wall,
@@ -347,11 +363,17 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": launches,
         "kernel_ms": {names[i]: float(kms[i]) for i in range(3)},
         "kernel_launches": {names[i]: int(klaunch[i]) for i in range(3)},
+        "kernel_share": {names[i]: float(kms[i] / kms.sum()) for i in range(3)},
+        "profiled_pass_s": prof_s,
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
+                     "bytes_per_launch": alg_bytes,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s"},
-        "pipeline_roofline": {"bytes_per_rotation": pipe_bytes, "achieved_gbs": pipe_bytes * value / world / 1e9,
-                              "frac": pipe_bytes * value / world / 1e9 / peak},
+        "pipeline_roofline": {"model": "streaming 3-pass, unpruned: 8N + 8H(2F+6) + (16H+17N)/B",
+                              "bytes_per_rotation": pipe_bytes, "achieved_gbs": pipe_bytes * value / world / 1e9,
+                              "frac": pipe_bytes * value / world / 1e9 / peak,
+                              "pruned_bytes_per_rotation": pruned_bytes,
+                              "pruned_frac": pruned_bytes * value / world / 1e9 / peak},
     }
     if pool is not None:
         cv, cn, cdt = cpu_sample(pool, cores, target, template, mask, rot_all, cfg["laplace"], args.cpu_rot_per_core)

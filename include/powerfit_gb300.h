@@ -83,6 +83,11 @@ int pf_set_stream(pf_ctx *ctx, void *stream);
  * (0 keeps the current value). */
 int pf_set_tuning(pf_ctx *ctx, int pairs_per_batch, int rows_pass1, int rows_pass3);
 int pf_get_tuning(const pf_ctx *ctx, int *pairs_per_batch, int *rows_pass1, int *rows_pass3);
+/* Autotuner: times short scans (trial_rotations of the uploaded set) over
+ * candidate batch and tile sizes and keeps the fastest; resets the results.
+ * No reference counterpart (the reference has no tunables). */
+int pf_autotune(pf_ctx *ctx, int64_t trial_rotations, int *pairs_per_batch, int *rows_pass1,
+                int *rows_pass3, double *best_ms);
 /* Radius beyond which rotated data is zero (pruning), planes kept, rmax. */
 int pf_get_geometry(const pf_ctx *ctx, int *reff, int *valid_planes, int *rmax);
 

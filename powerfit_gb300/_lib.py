@@ -22,7 +22,7 @@ PF_FLAG_GENERIC = 8
 EXPORTS = [
     "pf_create", "pf_destroy", "pf_last_error", "pf_global_error", "pf_set_target",
     "pf_set_template_mask", "pf_scan", "pf_set_rotations", "pf_reset_results",
-    "pf_scan_resident", "pf_get_results", "pf_synchronize", "pf_set_stream", "pf_set_tuning", "pf_get_tuning",
+    "pf_scan_resident", "pf_get_results", "pf_synchronize", "pf_set_stream", "pf_set_tuning", "pf_get_tuning", "pf_autotune",
     "pf_get_geometry", "pf_set_profiling", "pf_get_kernel_times", "pf_fft3d",
     "pf_rotate_grid3d", "pf_conj_multiply", "pf_calc_lcc", "pf_combine",
 ]
@@ -81,6 +81,8 @@ def load(path=None):
             "pf_set_stream": (_i, [_vp, _vp]),
             "pf_set_tuning": (_i, [_vp, _i, _i, _i]),
             "pf_get_tuning": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+            "pf_autotune": (_i, [_vp, _i64, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i),
+                                 ctypes.POINTER(_d)]),
             "pf_get_geometry": (_i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
             "pf_set_profiling": (_i, [_vp, _i]),
             "pf_get_kernel_times": (_i, [_vp, _vp, _vp]),
@@ -207,6 +209,14 @@ class Context:
         a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         self._call("pf_get_tuning", ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
         return a.value, b.value, c.value
+
+    def autotune(self, trial_rotations=512):
+        """Pick pairs per batch and tile rows by timing short scans (resets results)."""
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        ms = ctypes.c_double()
+        self._call("pf_autotune", int(trial_rotations), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                   ctypes.byref(ms))
+        return dict(pairs=a.value, rows1=b.value, rows3=c.value, trial_ms=ms.value)
 
     def get_geometry(self):
         a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

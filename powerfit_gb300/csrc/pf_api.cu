@@ -176,8 +176,8 @@ void choose_tiles(pf_ctx* c) {
   c->ty1 = ty;
   // pass 3: every voxel of a tile owned by one thread slot; enough tiles to
   // fill the machine (>= 4 per SM on 152 SMs)
-  int ty3 = ty;
-  while (ty3 > 1 && (long long)ty3 * X > (long long)kMaxVoxPerThread * kThreadsLine) ty3--;
+  int ty3 = 16;   // a power of two (the fast pass 3 splits tile indices with shifts)
+  while (ty3 > 1 && (long long)ty3 * X > (long long)kMaxVoxPerThread * kThreadsLine) ty3 /= 2;
   while (ty3 > 2 && (long long)c->nz * ((c->ny + ty3 - 1) / ty3) < 4 * 152) ty3 /= 2;
   c->ty3 = ty3;
   // pairs per batch: intermediate spectra of one batch <= 64 MiB (L2-sized), at least 1, at most 16
@@ -256,14 +256,24 @@ int timed_launch(pf_ctx* c, int which, Launch&& launch) {
   return PF_OK;
 }
 
+template <class K>
+cudaError_t allow_smem(K kernel, size_t total) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, kernel);
+  if (e != cudaSuccess) return e;
+  const size_t dyn = total > a.sharedSizeBytes ? total - a.sharedSizeBytes : 0;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+}
+
 int set_smem_limits(pf_ctx* c) {
-  const size_t s1 = line_smem(c->nx, 3, 16);
-  const size_t s2 = plane_smem(c->ny, c->nz);
-  PF_CUDA(c, cudaFuncSetAttribute(k_pass1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(s1, (size_t)48 * 1024)));
-  PF_CUDA(c, cudaFuncSetAttribute(k_pass3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(s1, (size_t)48 * 1024)));
-  PF_CUDA(c, cudaFuncSetAttribute(k_fwd_x_real, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(s1, (size_t)48 * 1024)));
-  PF_CUDA(c, cudaFuncSetAttribute(k_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
-  if (c->fast) PF_CUDA(c, c->fl.set_attrs(std::max(s1, (size_t)48 * 1024), s2));
+  // allow every kernel the device's opt-in maximum (static + dynamic); a
+  // launch only takes what it asks for
+  const size_t m = c->max_smem;
+  PF_CUDA(c, allow_smem(k_pass1, m));
+  PF_CUDA(c, allow_smem(k_pass3, m));
+  PF_CUDA(c, allow_smem(k_fwd_x_real, m));
+  PF_CUDA(c, allow_smem(k_pass2, m));
+  if (c->fast) PF_CUDA(c, c->fl.set_attrs(m, m));
   return PF_OK;
 }
 
@@ -586,8 +596,9 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     Pass3Params p3{g, c->px, c->twx, c->buf, npairs, r0, end, rot_offset, c->lcc_mask, c->norm_factor,
                    c->lcc, c->rot, ty3, (flags & PF_FLAG_FP64_NORM) ? 1 : 0};
     dim3 g3(c->nz, (c->ny + ty3 - 1) / ty3, 1);
+    const size_t s3f = pass3_smem(c->nx, ty3, npairs > 1 ? 2 : 1);
     rc = timed_launch(c, 2, [&] {
-      if (fast) c->fl.pass3(p3, g3, s3, c->stream);
+      if (fast) c->fl.pass3(p3, g3, s3f, c->stream);
       else k_pass3<<<g3, kThreadsLine, s3, c->stream>>>(p3);
     });
     if (rc) return rc;
@@ -632,6 +643,7 @@ int pf_set_tuning(pf_ctx* c, int pairs, int rows1, int rows3) {
   if (rows1 && (!ok_rows(rows1) || rows1 > 32)) return fail(c, PF_E_ARG, "rows_pass1 %d too large for nx %d", rows1, c->nx);
   if (rows3 && (!ok_rows(rows3) || (long long)rows3 * c->nx > (long long)kMaxVoxPerThread * kThreadsLine))
     return fail(c, PF_E_ARG, "rows_pass3 %d too large for nx %d", rows3, c->nx);
+  if (rows3 && (rows3 & (rows3 - 1))) return fail(c, PF_E_ARG, "rows_pass3 must be a power of two");
   if (pairs) {
     DeviceGuard guard(c->device);
     cudaStreamSynchronize(c->stream);
@@ -642,6 +654,86 @@ int pf_set_tuning(pf_ctx* c, int pairs, int rows1, int rows3) {
   if (rows1) c->ty1 = rows1;
   if (rows3) c->ty3 = rows3;
   return PF_OK;
+}
+
+int pf_autotune(pf_ctx* c, int64_t trial_rotations, int* best_pairs, int* best_rows1, int* best_rows3,
+                double* best_ms) {
+  if (!c) return PF_E_ARG;
+  if (!c->have_target || !c->have_template || c->nrot < 1)
+    return fail(c, PF_E_STATE, "autotune needs the target, the template/mask and a rotation set");
+  DeviceGuard guard(c->device);
+  const int64_t trial = std::max<int64_t>(1, std::min<int64_t>(trial_rotations > 0 ? trial_rotations : 512, c->nrot));
+  cudaEvent_t e0, e1;
+  PF_CUDA(c, cudaEventCreate(&e0));
+  PF_CUDA(c, cudaEventCreate(&e1));
+  const bool prof = c->profiling;
+  c->profiling = false;
+  auto time_cfg = [&](int pairs, int r1, int r3, float* ms) -> int {
+    int rc = pf_set_tuning(c, pairs, r1, r3);
+    if (rc) return rc;
+    rc = pf_scan_resident(c, 0, trial, 0, 0);   // warm-up (also allocates)
+    if (rc) return rc;
+    float best = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {
+      cudaEventRecord(e0, c->stream);
+      rc = pf_scan_resident(c, 0, trial, 0, 0);
+      if (rc) return rc;
+      cudaEventRecord(e1, c->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) return fail(c, PF_E_CUDA, "autotune timing failed");
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      best = std::min(best, t);
+    }
+    *ms = best;
+    return PF_OK;
+  };
+  int bp = c->pairs, b1 = c->ty1, b3 = c->ty3;
+  float bms = 1e30f;
+  int rc = time_cfg(bp, b1, b3, &bms);
+  // pairs per batch, capped by free device memory (half of what is free)
+  size_t freeb = 0, totalb = 0;
+  cudaMemGetInfo(&freeb, &totalb);
+  const size_t per_pair = 3ull * c->N * sizeof(float2);
+  const int pair_cands[] = {1, 2, 3, 4, 6, 8, 12, 16};
+  for (int pc : pair_cands) {
+    if (rc) break;
+    if (pc == bp || (size_t)pc * per_pair > (size_t)c->buf_pairs * per_pair + freeb / 2) continue;
+    if (2LL * pc > 4 * trial) continue;
+    float ms;
+    rc = time_cfg(pc, b1, b3, &ms);
+    if (!rc && ms < bms) { bms = ms; bp = pc; }
+  }
+  const int row_cands[] = {2, 4, 8, 16, 32};
+  for (int r1 : row_cands) {
+    if (rc) break;
+    if (r1 == b1 || (long long)r1 * c->nx > (long long)kMaxVoxPerThread * kThreadsLine ||
+        line_smem(c->nx, 3, r1) > std::max(line_smem(c->nx, 3, 16), (size_t)48 * 1024))
+      continue;
+    float ms;
+    rc = time_cfg(bp, r1, b3, &ms);
+    if (!rc && ms < bms) { bms = ms; b1 = r1; }
+  }
+  for (int r3 : row_cands) {
+    if (rc) break;
+    if (r3 == b3 || (long long)r3 * c->nx > (long long)kMaxVoxPerThread * kThreadsLine ||
+        line_smem(c->nx, 3, r3) > std::max(line_smem(c->nx, 3, 16), (size_t)48 * 1024))
+      continue;
+    float ms;
+    rc = time_cfg(bp, b1, r3, &ms);
+    if (!rc && ms < bms) { bms = ms; b3 = r3; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->profiling = prof;
+  if (rc) return rc;
+  rc = pf_set_tuning(c, bp, b1, b3);
+  if (rc) return rc;
+  rc = pf_reset_results(c);
+  if (best_pairs) *best_pairs = bp;
+  if (best_rows1) *best_rows1 = b1;
+  if (best_rows3) *best_rows3 = b3;
+  if (best_ms) *best_ms = bms;
+  return rc;
 }
 
 int pf_get_tuning(const pf_ctx* c, int* pairs, int* rows1, int* rows3) {

@@ -161,4 +161,107 @@ __device__ __forceinline__ void ct_lines(int nlines, const float2* __restrict__ 
   __syncthreads();
 }
 
+
+// Forward stages 0 .. nst-2 in place (all but the last).
+template <int L, int NT, int EMAX, int S, class Mid>
+__device__ __forceinline__ void ct_fwd_head(int nlines, const float2* __restrict__ tw, const Mid& mid) {
+  constexpr CtPlan P = ct_plan(L);
+  if constexpr (S < P.nst - 1) {
+    constexpr int R = P.r[S];
+    constexpr int NS = ct_stage_ns(L, S);
+    ct_stage<R, false, L, NS, NT, EMAX>(nlines, tw, mid, mid, true);
+    __syncthreads();
+    ct_fwd_head<L, NT, EMAX, S + 1>(nlines, tw, mid);
+  }
+}
+
+// Reversed radix plan (any radix order is a valid Stockham plan): used for the
+// inverse transform that follows a forward one, so that the inverse's first
+// stage consumes exactly the values the forward's last stage produced.
+constexpr CtPlan ct_plan_rev(int n) {
+  CtPlan p = ct_plan(n);
+  CtPlan q = p;
+  for (int i = 0; i < p.nst; ++i) q.r[i] = p.r[p.nst - 1 - i];
+  return q;
+}
+
+constexpr int ct_stage_ns_rev(int n, int stage) {
+  CtPlan q = ct_plan_rev(n);
+  int ns = 1;
+  for (int i = 0; i < stage; ++i) ns *= q.r[i];
+  return ns;
+}
+
+// Generic stage with an explicit radix (for reversed plans).
+template <int L, bool INV, int NT, int EMAX, int S, class Mid>
+__device__ __forceinline__ void ct_rev_from(int nlines, const float2* __restrict__ tw, const Mid& mid) {
+  constexpr CtPlan Q = ct_plan_rev(L);
+  if constexpr (S < Q.nst) {
+    constexpr int R = Q.r[S];
+    constexpr int NS = ct_stage_ns_rev(L, S);
+    ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, mid, mid, true);
+    __syncthreads();
+    ct_rev_from<L, INV, NT, EMAX, S + 1>(nlines, tw, mid);
+  }
+}
+
+// Forward transform, pointwise product, inverse transform of `nlines` lines
+// held in shared memory (`mid`).  The forward's last stage, the product
+// ``mul(line, k, v)`` and the inverse's first stage (reversed plan) run on the
+// same registers: radix R_last with Ns = L/R_last stores y[j + r L/R], which
+// is exactly what a first stage (Ns = 1) of radix R_last loads.
+template <int L, int NT, int EMAX, class Mid, class Mul>
+__device__ __forceinline__ void ct_fwd_mul_inv(int nlines, const float2* __restrict__ tw, const Mid& mid,
+                                               const Mul& mul) {
+  constexpr CtPlan P = ct_plan(L);
+  constexpr int RL = P.r[P.nst - 1];
+  constexpr int NB = L / RL;
+  // forward stages 0 .. nst-2
+  ct_fwd_head<L, NT, EMAX, 0>(nlines, tw, mid);
+  // fused stage
+  constexpr int KMAX = (EMAX / RL) > 0 ? (EMAX / RL) : 1;
+  constexpr int C0 = (NT * KMAX) / NB;
+  constexpr int C = ct_floor_pow2(C0 > 0 ? C0 : 1);
+  constexpr int K = (C * NB + NT - 1) / NT;
+  for (int l0 = 0; l0 < nlines; l0 += C) {
+    float2 v[K][RL];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int it = threadIdx.x + k * NT;
+      const int line = l0 + (it & (C - 1));
+      const int j = it / C;
+      if (j < NB && line < nlines) {
+        float2 m[RL];
+#pragma unroll
+        for (int r = 0; r < RL; ++r) m[r] = mul.fetch(line, j + r * NB);   // issue the operand loads early
+#pragma unroll
+        for (int r = 0; r < RL; ++r) v[k][r] = mid.load(line, j + r * NB);
+        if constexpr (NB > 1) {           // forward last stage twiddles (Ns = NB)
+          const int jm = j;               // (j % NB) * (L / (NB * RL)) with L / (NB * RL) == 1
+#pragma unroll
+          for (int r = 1; r < RL; ++r) v[k][r] = cmul(v[k][r], tw[r * jm]);
+        }
+        DFT<RL, false>::run(v[k]);
+#pragma unroll
+        for (int r = 0; r < RL; ++r) v[k][r] = cmulc(v[k][r], m[r]);
+        DFT<RL, true>::run(v[k]);         // inverse first stage (Ns = 1): no twiddles
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int it = threadIdx.x + k * NT;
+      const int line = l0 + (it & (C - 1));
+      const int j = it / C;
+      if (j < NB && line < nlines) {
+#pragma unroll
+        for (int r = 0; r < RL; ++r) mid.store(line, j * RL + r, v[k][r]);
+      }
+    }
+    __syncthreads();
+  }
+  // inverse stages 1 .. nst-1 of the reversed plan
+  ct_rev_from<L, true, NT, EMAX, 1>(nlines, tw, mid);
+}
+
 }  // namespace pf

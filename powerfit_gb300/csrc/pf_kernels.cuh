@@ -99,6 +99,13 @@ __device__ __forceinline__ int round_fixed(long long q, const double* __restrict
   return (int)round(v);
 }
 
+// 0.32 fixed-point fraction -> float in [0, 1): the top 23 bits become the
+// mantissa of a float in [1, 2), minus 1 (exact; integer ops instead of a
+// conversion instruction)
+__device__ __forceinline__ float frac_to_float(unsigned int f) {
+  return __int_as_float(0x3f800000u | (f >> 9)) - 1.0f;
+}
+
 struct GatherSrc {
   const float* __restrict__ tmpl;   // template, float32, C order (z, y, x)
   const float* __restrict__ mask;   // mask, float32
@@ -113,9 +120,9 @@ __device__ __forceinline__ void gather_point(const Geometry& g, const GatherSrc&
   // trilinear (x, then y, then z, as the reference)
   {
     const int x0 = (int)(s.qx >> 32), y0 = (int)(s.qy >> 32), z0 = (int)(s.qz >> 32);
-    const float fx = (float)(unsigned int)(s.qx & 0xffffffffLL) * 2.3283064365386963e-10f;
-    const float fy = (float)(unsigned int)(s.qy & 0xffffffffLL) * 2.3283064365386963e-10f;
-    const float fz = (float)(unsigned int)(s.qz & 0xffffffffLL) * 2.3283064365386963e-10f;
+    const float fx = frac_to_float((unsigned int)s.qx);
+    const float fy = frac_to_float((unsigned int)s.qy);
+    const float fz = frac_to_float((unsigned int)s.qz);
     const int ix0 = wrap1(x0, g.nx), ix1 = wrap1(x0 + 1, g.nx);
     const long long iy0 = (long long)wrap1(y0, g.ny) * g.nx, iy1 = (long long)wrap1(y0 + 1, g.ny) * g.nx;
     const long long iz0 = (long long)wrap1(z0, g.nz) * sxy, iz1 = (long long)wrap1(z0 + 1, g.nz) * sxy;

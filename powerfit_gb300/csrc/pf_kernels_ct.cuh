@@ -6,6 +6,7 @@
 // rotation, so pass 1 neither transforms nor stores it and pass 2 reads zeros
 // for it without touching memory.
 #pragma once
+#include <algorithm>
 #include "pf_fft_ct.cuh"
 #include "pf_kernels.cuh"
 
@@ -56,16 +57,40 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass1_ct(const Pass1Params p, 
   const double* rdb = p.rotd + 9 * (has_b ? rb : 0);
   const int r2 = min(g.rmax, g.reff) * min(g.rmax, g.reff);
 
-  for (int v = threadIdx.x; v < p.ty * X; v += kThreadsLine) {
-    const int r = v / X, x = v - r * X;
-    float ta = 0.f, ma = 0.f, tb = 0.f, mb = 0.f;
-    if ((rowmask >> r) & 1u) {
-      const int cy = signed_coord(y0 + r, g.ny), cx = signed_coord(x, X);
-      if (cz * cz + cy * cy + cx * cx <= r2) {
-        if (has_a) gather_point(g, p.src, Ra, rda, cz, cy, cx, ta, ma);
-        if (has_b) gather_point(g, p.src, Rb, rdb, cz, cy, cx, tb, mb);
+  // zero the tile, then gather only the points inside the sphere, spread
+  // evenly over the threads (rows near the rim hold few points)
+  for (int v = threadIdx.x; v < 3 * p.ty * rs; v += kThreadsLine) fld[v] = make_float2(0.f, 0.f);
+  __shared__ int s_start[33];
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int r = 0; r < p.ty; ++r) {
+      s_start[r] = acc;
+      if ((rowmask >> r) & 1u) {
+        const int cy = signed_coord(y0 + r, g.ny);
+        const int rem = r2 - cz * cz - cy * cy;
+        int xr = (int)sqrtf((float)rem);
+        while (xr * xr > rem) --xr;
+        while ((xr + 1) * (xr + 1) <= rem) ++xr;
+        acc += (2 * xr + 1 >= X) ? X : 2 * xr + 1;
       }
     }
+    s_start[p.ty] = acc;
+  }
+  __syncthreads();
+  const int total = s_start[p.ty];
+  for (int k = threadIdx.x; k < total; k += kThreadsLine) {
+    int r = 0;
+#pragma unroll
+    for (int i = 1; i < 32; ++i) r += (i < p.ty && k >= s_start[i]) ? 1 : 0;
+    const int i = k - s_start[r];
+    const int n_r = s_start[r + 1] - s_start[r];
+    int x, cx;
+    if (n_r == X) { x = i; cx = signed_coord(i, X); }
+    else { cx = i - (n_r - 1) / 2; x = cx < 0 ? cx + X : cx; }
+    const int cy = signed_coord(y0 + r, g.ny);
+    float ta = 0.f, ma = 0.f, tb = 0.f, mb = 0.f;
+    if (has_a) gather_point(g, p.src, Ra, rda, cz, cy, cx, ta, ma);
+    if (has_b) gather_point(g, p.src, Rb, rdb, cz, cy, cx, tb, mb);
     fld[(0 * p.ty + r) * rs + x] = make_float2(ta, -ma);
     fld[(1 * p.ty + r) * rs + x] = make_float2(tb, -mb);
     fld[(2 * p.ty + r) * rs + x] = make_float2(ma * ma, -(mb * mb));
@@ -79,16 +104,26 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass1_ct(const Pass1Params p, 
 // ---------------------------------------------------------------------------
 // Pass 2 (fast): (z, y) plane per (pair, field, kx)
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+struct SpectrumOperand {  // target spectrum plane [kz][ky] of this kx
+  const float2* __restrict__ spec;
+  int ny;
+  __device__ __forceinline__ float2 fetch(int ky, int kz) const { return __ldg(spec + (long long)kz * ny + ky); }
+};
+
 template <int Y, int Z>
-__global__ void __launch_bounds__(kThreadsPlane) k_pass2_ct(const Pass2Params p, const int re2) {
+__global__ void __launch_bounds__(kThreadsPlane, 1) k_pass2_ct(const Pass2Params p, const int re2) {
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
   constexpr int rs = Y + kPad;
   float2* twy = sm;
   float2* twz = sm + Y;
   float2* pl = sm + Y + Z;
-  for (int i = threadIdx.x; i < Y; i += kThreadsPlane) twy[i] = p.twy[i];
-  for (int i = threadIdx.x; i < Z; i += kThreadsPlane) twz[i] = p.twz[i];
 
   const int kx = blockIdx.x, f = blockIdx.y, pair = blockIdx.z;
   constexpr long long plane = (long long)Z * Y;
@@ -96,19 +131,18 @@ __global__ void __launch_bounds__(kThreadsPlane) k_pass2_ct(const Pass2Params p,
   const int nvz = g.nvz;
   const int lo_end = g.zlo, hi_start = Z - (nvz - g.zlo - 1);
 
-  if (p.mode == 0) {
-    for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlane) {
-      const int z = v / Y, y = v - z * Y;
-      const bool valid = (z <= lo_end || z >= hi_start) &&
-                         row_in_disk(g, signed_coord(z, Z), signed_coord(y, Y), re2);
-      pl[z * rs + y] = valid ? gplane[(long long)z * Y + y] : make_float2(0.f, 0.f);
-    }
-  } else {
-    for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlane) {
-      const int z = v / Y, y = v - z * Y;
-      pl[z * rs + y] = gplane[(long long)z * Y + y];
-    }
+  // copy-in: asynchronous 8-byte copies of the rows the rotation can reach,
+  // zeros elsewhere (every thread keeps many copies in flight)
+  for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlane) {
+    const int z = v / Y, y = v - z * Y;
+    const bool valid = p.mode != 0 ||
+                       ((z <= lo_end || z >= hi_start) && row_in_disk(g, signed_coord(z, Z), signed_coord(y, Y), re2));
+    if (valid) cp_async8(pl + z * rs + y, gplane + (long long)z * Y + y);
+    else pl[z * rs + y] = make_float2(0.f, 0.f);
   }
+  for (int i = threadIdx.x; i < Y; i += kThreadsPlane) twy[i] = p.twy[i];
+  for (int i = threadIdx.x; i < Z; i += kThreadsPlane) twz[i] = p.twz[i];
+  cp_async_wait_all();
   __syncthreads();
 
   RowMapLines rows{pl, rs, g.zlo, Z - nvz};
@@ -116,11 +150,10 @@ __global__ void __launch_bounds__(kThreadsPlane) k_pass2_ct(const Pass2Params p,
   SmemLines cols{pl, 1, rs};
   if (p.mode == 0) {
     const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + (long long)kx * plane;
-    ProductStore prod{pl, rs, spec, Y};
-    ct_lines<Z, false, kThreadsPlane, kEmax>(Y, twz, cols, cols, prod, true, true);
-    ct_lines<Z, true, kThreadsPlane, kEmax>(Y, twz, cols, cols, cols, true, true);
+    ct_fwd_mul_inv<Z, kThreadsPlane, kEmax>(Y, twz, cols, SpectrumOperand{spec, Y});
     SmemLines allrows{pl, rs, 1};
     ct_lines<Y, true, kThreadsPlane, kEmax>(Z, twy, allrows, allrows, allrows, true, true);
+#pragma unroll 4
     for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlane) {
       const int z = v / Y, y = v - z * Y;
       gplane[(long long)z * Y + y] = pl[z * rs + y];
@@ -138,16 +171,31 @@ __global__ void __launch_bounds__(kThreadsPlane) k_pass2_ct(const Pass2Params p,
 // ---------------------------------------------------------------------------
 // Pass 3 (fast): inverse x transform, LCC, running max / argmax
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Shared-memory bytes of pass 3 for `nbuf` tile buffers.
+__host__ __device__ inline size_t pass3_smem(int X, int ty, int nbuf) {
+  return ((size_t)X + (size_t)nbuf * 3 * ty * (X + kPad)) * sizeof(float2);
+}
+
 template <int X>
-struct GlobalRowsLoadCt {  // line = f*ty + r, idx = kx: buf[f][kx][z][y0 + r]
-  const float2* base;
-  int ty, y0, ny, nz, z;
-  __device__ __forceinline__ float2 load(int line, int idx) const {
-    const int f = line / ty, r = line - f * ty;
-    const int y = y0 + r;
-    return y < ny ? base[(((long long)f * X + idx) * nz + z) * ny + y] : make_float2(0.f, 0.f);
+__device__ __forceinline__ void pass3_prefetch(const float2* __restrict__ base, float2* fld, int ty, int y0, int ny,
+                                               int nz, int z) {
+  // buf[f][kx][z][y0 + r] -> fld[(f*ty + r)*rs + kx]; consecutive threads take consecutive rows (y)
+  constexpr int rs = X + kPad;
+  const int n = 3 * ty * X;
+  const int sh = __ffs(ty) - 1;         // ty is a power of two on this path
+  for (int v = threadIdx.x; v < n; v += kThreadsLine) {
+    const int r = v & (ty - 1);
+    const int fk = v >> sh;             // f * X + kx
+    const int f = fk / X, kx = fk - f * X;
+    float2* dst = fld + (f * ty + r) * rs + kx;
+    if (y0 + r < ny) cp_async8(dst, base + (((long long)f * X + kx) * nz + z) * ny + (y0 + r));
+    else *dst = make_float2(0.f, 0.f);
   }
-};
+}
 
 template <int X>
 __global__ void __launch_bounds__(kThreadsLine, 2) k_pass3_ct(const Pass3Params p) {
@@ -155,13 +203,19 @@ __global__ void __launch_bounds__(kThreadsLine, 2) k_pass3_ct(const Pass3Params 
   const Geometry& g = p.g;
   constexpr int rs = X + kPad;
   float2* tw = sm;
-  float2* fld = sm + X;
-  for (int i = threadIdx.x; i < X; i += kThreadsLine) tw[i] = p.twx[i];
+  float2* fbuf0 = sm + X;
+  const int fbuf_stride = 3 * p.ty * rs;
 
   const int z = blockIdx.x;
   const int y0 = blockIdx.y * p.ty;
   const int nvox = p.ty * X;
   const long long zoff = (long long)z * g.ny * X;
+  const long long fstride = (long long)X * g.nz * g.ny;
+
+  // start the first tile's copies before anything else
+  pass3_prefetch<X>(p.buf, fbuf0, p.ty, y0, g.ny, g.nz, z);
+  cp_async_commit();
+  for (int i = threadIdx.x; i < X; i += kThreadsLine) tw[i] = p.twx[i];
 
   float best[kMaxVoxPerThread];
   int brot[kMaxVoxPerThread];
@@ -183,11 +237,19 @@ __global__ void __launch_bounds__(kThreadsLine, 2) k_pass3_ct(const Pass3Params 
     }
   }
 
-  const long long fstride = (long long)X * g.nz * g.ny;
   for (int pair = 0; pair < p.npairs; ++pair) {
-    GlobalRowsLoadCt<X> src{p.buf + (long long)pair * 3 * fstride, p.ty, y0, g.ny, g.nz, z};
+    float2* fld = fbuf0 + (pair & 1) * fbuf_stride;
+    if (pair + 1 < p.npairs) {
+      pass3_prefetch<X>(p.buf + (long long)(pair + 1) * 3 * fstride, fbuf0 + ((pair + 1) & 1) * fbuf_stride, p.ty, y0,
+                        g.ny, g.nz, z);
+      cp_async_commit();
+      cp_async_wait_group<1>();
+    } else {
+      cp_async_wait_group<0>();
+    }
+    __syncthreads();
     SmemLines lines{fld, rs, 1};
-    ct_lines<X, true, kThreadsLine, kEmax>(3 * p.ty, tw, src, lines, lines, false, true);
+    ct_lines<X, true, kThreadsLine, kEmax>(3 * p.ty, tw, lines, lines, lines, true, true);
     const long long ra = p.first_rot + 2LL * pair;
     const bool has_b = ra + 1 < p.nrot;
 #pragma unroll
@@ -246,12 +308,19 @@ struct FastSize {
   static void pass3(const Pass3Params& p, dim3 grid, size_t smem, cudaStream_t s) {
     k_pass3_ct<N><<<grid, kThreadsLine, smem, s>>>(p);
   }
+  template <class K>
+  static cudaError_t allow_smem(K kernel, size_t bytes) {
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, kernel);
+    if (e != cudaSuccess) return e;
+    const size_t dyn = bytes > a.sharedSizeBytes ? bytes - a.sharedSizeBytes : 0;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  }
+  // `smem_line` / `smem_plane`: total shared memory (static + dynamic) each kernel may use
   static cudaError_t set_attrs(size_t smem_line, size_t smem_plane) {
-    cudaError_t e = cudaFuncSetAttribute(k_pass1_ct<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_line);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_pass3_ct<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_line);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_pass2_ct<N, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_plane);
+    cudaError_t e = allow_smem(k_pass1_ct<N>, smem_line);
+    if (e == cudaSuccess) e = allow_smem(k_pass3_ct<N>, smem_line);
+    if (e == cudaSuccess) e = allow_smem(k_pass2_ct<N, N>, smem_plane);
     return e;
   }
   static FastLaunch table() { return FastLaunch{&pass1, &pass2, &pass3, &set_attrs}; }

@@ -248,3 +248,17 @@ def test_fast_path_equals_generic(lib, n):
     assert np.max(np.abs(corr.lcc - lg)) <= 1e-6
     upd = np.abs(corr.lcc - lg) == 0
     assert np.mean(corr.rot[upd] == rg[upd]) == 1.0
+
+
+def test_autotune_keeps_results(lib):
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    target, template, mask = _synthetic((64, 64, 64), 2.0, 1000, 8.0, 6, False)
+    rot = quat_to_rotmat(super_fibonacci(41))
+    base = correlator(target, template, mask, rot, False)
+    ctx = base.context
+    ctx.set_rotations(rot)
+    cfg = ctx.autotune(40)
+    assert cfg["pairs"] >= 1 and cfg["rows1"] >= 1 and cfg["rows3"] >= 1
+    assert cfg["rows3"] & (cfg["rows3"] - 1) == 0
+    lcc, r = ctx.scan(rot)
+    assert np.array_equal(lcc, base.lcc) and np.array_equal(r, base.rot)
