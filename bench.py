@@ -219,7 +219,10 @@ def run_ours(args, rank, world, local_rank):
     ctx = _lib.Context(shape, local_rank)
     if args.pairs:
         ctx.set_tuning(pairs=args.pairs)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream made current: the library launches on it
+    # and the CUDA events below are recorded on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     ctx.set_target(ftarget, base._lcc_mask)
     ctx.set_template_mask(base._template, base._mask, float(base._norm_factor), base._rmax)

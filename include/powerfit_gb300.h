@@ -76,7 +76,9 @@ int pf_scan_resident(pf_ctx *ctx, int64_t first, int64_t count, int64_t rot_offs
 int pf_get_results(pf_ctx *ctx, float *out_lcc, int32_t *out_rot);
 int pf_synchronize(pf_ctx *ctx);
 /* Launch on the caller's cudaStream_t (NULL: back to the context's own
- * stream); lets a host framework order the search with its own work. */
+ * non-blocking stream -- so the legacy default stream cannot be selected;
+ * pass a created stream); lets a host framework order the search with its
+ * own work and time it with events on that stream. */
 int pf_set_stream(pf_ctx *ctx, void *stream);
 
 /* Tuning: rotation pairs per batch, rows per tile of passes 1 and 3

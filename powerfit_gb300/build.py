@@ -49,7 +49,8 @@ def up_to_date():
 
 def _compile(src, verbose):
     obj = os.path.join(OBJ_DIR, os.path.basename(src)[:-3] + ".o")
-    cmd = [nvcc()] + ARCH + FLAGS + ["-c", src, "-o", obj]
+    extra = os.environ.get("POWERFIT_NVCC_FLAGS", "").split()   # build-variant knob (e.g. -DPF_PACKED_F32X2=0)
+    cmd = [nvcc()] + ARCH + FLAGS + extra + ["-c", src, "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     res = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)

@@ -109,6 +109,9 @@ struct pf_ctx {
   long long buf_pairs = 0;
   RotFixed* rots = nullptr;
   double* rotd = nullptr;
+  int4* rows_reach = nullptr;       // fast pass 1: rows inside the reach disk (pruned)
+  int4* rows_full = nullptr;        // fast pass 1: rows inside the rmax disk (no pruning)
+  int nrows_reach = 0, nrows_full = 0;
   long long nrot = 0, rot_cap = 0;
   Geometry g{};
   int rmax = 0, reff_data = 0;
@@ -288,6 +291,33 @@ bool fast_table(int n, FastLaunch* fl) {
   }
 }
 
+// (z, y, points in the sphere) of every row with cz^2 + cy^2 <= re^2, z-major
+int build_rows(pf_ctx* c, int re, int4** dptr, int* count) {
+  std::vector<int4> rows;
+  const long long re2 = (long long)re * re;
+  for (int z = 0; z < c->nz; ++z) {
+    const int cz = (2 * z <= c->nz) ? z : z - c->nz;
+    for (int y = 0; y < c->ny; ++y) {
+      const int cy = (2 * y <= c->ny) ? y : y - c->ny;
+      const long long rem = re2 - (long long)cz * cz - (long long)cy * cy;
+      if (rem < 0) continue;
+      long long xr = (long long)std::sqrt((double)rem);
+      while (xr * xr > rem) --xr;
+      while ((xr + 1) * (xr + 1) <= rem) ++xr;
+      const int cnt = (2 * xr + 1 >= c->nx) ? c->nx : (int)(2 * xr + 1);
+      rows.push_back(make_int4(z, y, cnt, 0));
+    }
+  }
+  if (*dptr) cudaFree(*dptr);
+  *dptr = nullptr;
+  *count = (int)rows.size();
+  if (rows.empty()) return PF_OK;
+  int rc = alloc(c, (void**)dptr, rows.size() * sizeof(int4));
+  if (rc) return rc;
+  PF_CUDA(c, cudaMemcpy(*dptr, rows.data(), rows.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  return PF_OK;
+}
+
 int upload_double_as_float(pf_ctx* c, float* dst, const double* src, long long n) {
   std::vector<float> tmp((size_t)n);
   for (long long i = 0; i < n; ++i) tmp[i] = (float)src[i];
@@ -430,7 +460,8 @@ int pf_destroy(pf_ctx* c) {
   for (auto e : c->ev_pool) cudaEventDestroy(e);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   c->own_stream = nullptr;
-  void* ptrs[] = {c->twx, c->twy, c->twz, c->tmpl, c->mask, c->lcc_mask, c->spec, c->lcc, c->rot, c->buf, c->rots, c->rotd};
+  void* ptrs[] = {c->twx, c->twy, c->twz, c->tmpl, c->mask, c->lcc_mask, c->spec, c->lcc, c->rot, c->buf, c->rots, c->rotd,
+                  c->rows_reach, c->rows_full};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete c;
@@ -496,6 +527,11 @@ int pf_set_template_mask(pf_ctx* c, const double* tmpl, const double* mask, doub
   if (rs + 1.0 < nmin / 2.0) reff = std::min(rmax, (int)std::floor(rs + 1.7320508075688772 + 1e-6) + 1);
   c->reff_data = reff;
   compute_geometry(c, reff);
+  if (c->fast) {
+    int rc2 = build_rows(c, std::min(rmax, reff), &c->rows_reach, &c->nrows_reach);
+    if (!rc2) rc2 = build_rows(c, rmax, &c->rows_full, &c->nrows_full);
+    if (rc2) return rc2;
+  }
   c->have_template = true;
   return PF_OK;
 }
@@ -569,11 +605,19 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
   const int64_t end = first + count;
   for (int64_t r0 = first; r0 < end; r0 += 2LL * P) {
     const int npairs = (int)std::min<int64_t>(P, (end - r0 + 1) / 2);
-    Pass1Params p1{g, c->px, GatherSrc{c->tmpl, c->mask}, c->twx, c->rots, c->rotd, r0, end, c->buf, ty1};
-    dim3 g1(g.nvz, (c->ny + ty1 - 1) / ty1, npairs);
+    const bool full = (flags & PF_FLAG_NO_PRUNE) != 0;
+    Pass1Params p1{g, c->px, GatherSrc{c->tmpl, c->mask}, c->twx, c->rots, c->rotd, r0, end, c->buf, ty1,
+                   full ? c->rows_full : c->rows_reach, full ? c->nrows_full : c->nrows_reach};
     rc = timed_launch(c, 0, [&] {
-      if (fast) c->fl.pass1(p1, re2, g1, s1, c->stream);
-      else k_pass1<<<g1, kThreadsLine, s1, c->stream>>>(p1);
+      if (fast) {
+        if (p1.nrows > 0) {
+          dim3 g1((p1.nrows + ty1 - 1) / ty1, 1, npairs);
+          c->fl.pass1(p1, re2, g1, s1, c->stream);
+        }
+      } else {
+        dim3 g1(g.nvz, (c->ny + ty1 - 1) / ty1, npairs);
+        k_pass1<<<g1, kThreadsLine, s1, c->stream>>>(p1);
+      }
     });
     if (rc) return rc;
     Pass2Params p2{};
@@ -694,7 +738,7 @@ int pf_autotune(pf_ctx* c, int64_t trial_rotations, int* best_pairs, int* best_r
   size_t freeb = 0, totalb = 0;
   cudaMemGetInfo(&freeb, &totalb);
   const size_t per_pair = 3ull * c->N * sizeof(float2);
-  const int pair_cands[] = {1, 2, 3, 4, 6, 8, 12, 16};
+  const int pair_cands[] = {1, 2, 4, 8, 16, 24, 32, 48, 64};
   for (int pc : pair_cands) {
     if (rc) break;
     if (pc == bp || (size_t)pc * per_pair > (size_t)c->buf_pairs * per_pair + freeb / 2) continue;

@@ -55,8 +55,43 @@ __host__ __device__ constexpr double ct_twi(int m, int n, bool inv) {
   return inv ? s : -s;
 }
 
+// Complex add / subtract.  With PF_PACKED_F32X2 (the default) they use the
+// packed two-lane FP32 instructions of sm_100+ (add/sub.rn.f32x2): one issue
+// slot per complex add instead of two, the same rounding as two scalar adds.
+#ifndef PF_PACKED_F32X2
+#define PF_PACKED_F32X2 1
+#endif
+
+#if PF_PACKED_F32X2
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+  float2 d;
+  asm("{\n .reg .b64 ra, rb, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n"
+      " add.rn.f32x2 rd, ra, rb;\n mov.b64 {%0, %1}, rd;\n}\n"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+  float2 d;
+  asm("{\n .reg .b64 ra, rb, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n"
+      " sub.rn.f32x2 rd, ra, rb;\n mov.b64 {%0, %1}, rd;\n}\n"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+// a + b * (s0, s1) per lane (fused multiply-add, packed)
+__device__ __forceinline__ float2 cfma_lanes(float2 b, float s0, float s1, float2 a) {
+  float2 d;
+  asm("{\n .reg .b64 ra, rb, rs, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n"
+      " mov.b64 rs, {%6, %7};\n fma.rn.f32x2 rd, rb, rs, ra;\n mov.b64 {%0, %1}, rd;\n}\n"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(s0), "f"(s1));
+  return d;
+}
+#else
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cfma_lanes(float2 b, float s0, float s1, float2 a) {
+  return make_float2(fmaf(b.x, s0, a.x), fmaf(b.y, s1, a.y));
+}
+#endif
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -190,7 +225,21 @@ template <int A, int B, bool INV> struct DFTComposite {
     }
   }
 };
-template <bool INV> struct DFT<4, INV> : DFTComposite<2, 2, INV> {};
+// radix 4: X0 = (a+c)+(b+d), X2 = (a+c)-(b+d), X1 = (a-c) -+ i(b-d), X3 = (a-c) +- i(b-d)
+// (forward upper signs); the +-i products are a swap of (b-d) and one packed
+// multiply-add by (1, -1) or (-1, 1)
+template <bool INV> struct DFT<4, INV> {
+  __device__ __forceinline__ static void run(float2* v) {
+    const float2 s0 = cadd(v[0], v[2]), d0 = csub(v[0], v[2]);
+    const float2 s1 = cadd(v[1], v[3]), d1 = csub(v[1], v[3]);
+    const float2 sw = make_float2(d1.y, d1.x);
+    v[0] = cadd(s0, s1);
+    v[2] = csub(s0, s1);
+    // forward: X1 = d0 - i d1 = (d0.x + d1.y, d0.y - d1.x)
+    v[1] = INV ? cfma_lanes(sw, -1.f, 1.f, d0) : cfma_lanes(sw, 1.f, -1.f, d0);
+    v[3] = INV ? cfma_lanes(sw, 1.f, -1.f, d0) : cfma_lanes(sw, -1.f, 1.f, d0);
+  }
+};
 template <bool INV> struct DFT<6, INV> : DFTComposite<2, 3, INV> {};
 template <bool INV> struct DFT<8, INV> : DFTComposite<4, 2, INV> {};
 template <bool INV> struct DFT<10, INV> : DFTComposite<2, 5, INV> {};

@@ -159,6 +159,8 @@ struct Pass1Params {
   long long nrot;                       // total rotations of this scan
   float2* __restrict__ buf;             // intermediate spectra
   int ty;                               // rows per tile
+  const int4* __restrict__ rows;        // fast path: (z, y, points in the sphere, 0) of every reachable row
+  int nrows;
 };
 
 struct TransposedStore {  // line = f*ty + r  (row y0 + r of field f); idx = kx
@@ -344,7 +346,9 @@ __device__ __forceinline__ float lcc_value(float gcc, float ave, float ave2, flo
   const float bb = s - p1;
   const float err = (p1 - (s - bb)) + (-p2 - bb);
   const float var = s + ((err + e1) - e2);
-  return gcc / sqrtf(var);
+  // rsqrt keeps the IEEE cases of gcc / sqrt(var): var == 0 -> +-inf (NaN for
+  // gcc == 0), var < 0 -> NaN
+  return gcc * rsqrtf(var);
 }
 
 __device__ __forceinline__ float lcc_value64(float gcc, float ave, float ave2, float nm) {

@@ -20,16 +20,22 @@ __device__ __forceinline__ bool row_in_disk(const Geometry& g, int cz, int cy, i
 // Pass 1 (fast): gather + forward x transform of rows inside the disk
 // ---------------------------------------------------------------------------
 template <int X>
-struct DiskTransposedStore {  // line = f*ty + r; idx = kx; rows outside the disk are skipped
+struct RowListStore {  // line = f*ty + c (row c of the chunk); idx = kx
   float2* base;
-  int ty, y0, ny, nz, z;
-  unsigned int rowmask;        // bit r set: row y0 + r is inside the disk
+  const int4* rows;    // shared-memory copy of the chunk's row entries
+  int ty, nr, ny, nz;
   __device__ __forceinline__ void store(int line, int idx, float2 v) const {
-    const int f = line / ty, r = line - f * ty;
-    if ((rowmask >> r) & 1u) base[(((long long)f * X + idx) * nz + z) * ny + (y0 + r)] = v;
+    const int f = line / ty, c = line - f * ty;
+    if (c < nr) {
+      const int4 e = rows[c];
+      base[(((long long)f * X + idx) * nz + e.x) * ny + e.y] = v;
+    }
   }
 };
 
+// Pass 1 over a list of the (z, y) rows the rotation can reach (built on the
+// host from the template's support): every block transforms `ty` such rows,
+// none is empty and none is outside the reach.
 template <int X>
 __global__ void __launch_bounds__(kThreadsLine) k_pass1_ct(const Pass1Params p, const int re2) {
   extern __shared__ float2 sm[];
@@ -37,16 +43,22 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass1_ct(const Pass1Params p, 
   constexpr int rs = X + kPad;
   float2* tw = sm;
   float2* fld = sm + X;
-  const int z = valid_plane(g, blockIdx.x);
-  const int cz = signed_coord(z, g.nz);
-  const int y0 = blockIdx.y * p.ty;
-  unsigned int rowmask = 0;
-  for (int r = 0; r < p.ty; ++r) {
-    const int y = y0 + r;
-    if (y < g.ny && row_in_disk(g, cz, signed_coord(y, g.ny), re2)) rowmask |= 1u << r;
-  }
-  if (rowmask == 0) return;                 // whole tile outside the disk (uniform per block)
+  __shared__ int4 s_row[32];
+  __shared__ int s_start[33];
+  const int c0 = blockIdx.x * p.ty;
+  const int nr = min(p.ty, p.nrows - c0);
+  if (threadIdx.x < nr) s_row[threadIdx.x] = p.rows[c0 + threadIdx.x];
   for (int i = threadIdx.x; i < X; i += kThreadsLine) tw[i] = p.twx[i];
+  for (int v = threadIdx.x; v < 3 * p.ty * rs; v += kThreadsLine) fld[v] = make_float2(0.f, 0.f);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int c = 0; c < p.ty; ++c) {
+      s_start[c] = acc;
+      if (c < nr) acc += s_row[c].z;
+    }
+    s_start[p.ty] = acc;
+  }
 
   const int pair = blockIdx.z;
   const long long ra = p.first_rot + 2LL * pair, rb = ra + 1;
@@ -55,49 +67,30 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass1_ct(const Pass1Params p, 
   const RotFixed Rb = p.rots[has_b ? rb : 0];
   const double* rda = p.rotd + 9 * (has_a ? ra : 0);
   const double* rdb = p.rotd + 9 * (has_b ? rb : 0);
-  const int r2 = min(g.rmax, g.reff) * min(g.rmax, g.reff);
-
-  // zero the tile, then gather only the points inside the sphere, spread
-  // evenly over the threads (rows near the rim hold few points)
-  for (int v = threadIdx.x; v < 3 * p.ty * rs; v += kThreadsLine) fld[v] = make_float2(0.f, 0.f);
-  __shared__ int s_start[33];
-  if (threadIdx.x == 0) {
-    int acc = 0;
-    for (int r = 0; r < p.ty; ++r) {
-      s_start[r] = acc;
-      if ((rowmask >> r) & 1u) {
-        const int cy = signed_coord(y0 + r, g.ny);
-        const int rem = r2 - cz * cz - cy * cy;
-        int xr = (int)sqrtf((float)rem);
-        while (xr * xr > rem) --xr;
-        while ((xr + 1) * (xr + 1) <= rem) ++xr;
-        acc += (2 * xr + 1 >= X) ? X : 2 * xr + 1;
-      }
-    }
-    s_start[p.ty] = acc;
-  }
   __syncthreads();
+
+  // gather the points inside the sphere, spread evenly over the threads
   const int total = s_start[p.ty];
   for (int k = threadIdx.x; k < total; k += kThreadsLine) {
-    int r = 0;
+    int c = 0;
 #pragma unroll
-    for (int i = 1; i < 32; ++i) r += (i < p.ty && k >= s_start[i]) ? 1 : 0;
-    const int i = k - s_start[r];
-    const int n_r = s_start[r + 1] - s_start[r];
+    for (int i = 1; i < 32; ++i) c += (i < p.ty && k >= s_start[i]) ? 1 : 0;
+    const int i = k - s_start[c];
+    const int4 e = s_row[c];
     int x, cx;
-    if (n_r == X) { x = i; cx = signed_coord(i, X); }
-    else { cx = i - (n_r - 1) / 2; x = cx < 0 ? cx + X : cx; }
-    const int cy = signed_coord(y0 + r, g.ny);
+    if (e.z == X) { x = i; cx = signed_coord(i, X); }
+    else { cx = i - (e.z - 1) / 2; x = cx < 0 ? cx + X : cx; }
+    const int cz = signed_coord(e.x, g.nz), cy = signed_coord(e.y, g.ny);
     float ta = 0.f, ma = 0.f, tb = 0.f, mb = 0.f;
     if (has_a) gather_point(g, p.src, Ra, rda, cz, cy, cx, ta, ma);
     if (has_b) gather_point(g, p.src, Rb, rdb, cz, cy, cx, tb, mb);
-    fld[(0 * p.ty + r) * rs + x] = make_float2(ta, -ma);
-    fld[(1 * p.ty + r) * rs + x] = make_float2(tb, -mb);
-    fld[(2 * p.ty + r) * rs + x] = make_float2(ma * ma, -(mb * mb));
+    fld[(0 * p.ty + c) * rs + x] = make_float2(ta, -ma);
+    fld[(1 * p.ty + c) * rs + x] = make_float2(tb, -mb);
+    fld[(2 * p.ty + c) * rs + x] = make_float2(ma * ma, -(mb * mb));
   }
   __syncthreads();
   SmemLines lines{fld, rs, 1};
-  DiskTransposedStore<X> out{p.buf + (long long)pair * 3 * X * g.nz * g.ny, p.ty, y0, g.ny, g.nz, z, rowmask};
+  RowListStore<X> out{p.buf + (long long)pair * 3 * X * g.nz * g.ny, s_row, p.ty, nr, g.ny, g.nz};
   ct_lines<X, false, kThreadsLine, kEmax>(3 * p.ty, tw, lines, lines, out, true, false);
 }
 
