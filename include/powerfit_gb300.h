@@ -119,6 +119,23 @@ int pf_calc_lcc(const double *gcc, const double *ave, const double *ave2, const 
 int pf_combine(float *lcc, int32_t *rot, const float *part_lcc, const int32_t *part_rot,
                int64_t n, int64_t rot_add);
 
+/* --- preprocessing on the GPU (run once per search; host arrays) -------- */
+/* _powerfit.pyx:75-140 (blur_points): out += w exp(-d^2 / 2 sigma^2) within
+ * 4 sigma of each point; points are (3, n) rows x, y, z in voxel units; with
+ * wraparound negative indices wrap once (as the reference's Cython indexing). */
+int pf_blur_points(const double *points, const double *weights, int64_t n, double sigma, double *out,
+                   int nz, int ny, int nx, int wraparound);
+/* _powerfit.pyx:143-206 (dilate_points): out = 1 within radii[i] of each point. */
+int pf_dilate_points(const double *points, const double *radii, int64_t n, double *out,
+                     int nz, int ny, int nx, int wraparound);
+/* powerfitter.py:212-215: scipy.ndimage.laplace(in, mode='wrap'). */
+int pf_laplace_wrap(const double *in, double *out, int nz, int ny, int nx);
+/* helpers.py:26-34 (determine_core_indices): number of 6-connected binary
+ * erosions (border 0) each voxel of mask > 0 survives, counting itself. */
+int pf_core_indices(const double *mask, double *out, int nz, int ny, int nx);
+/* message of the last failing preprocessing call */
+int pf_prep_error(char *buf, size_t len);
+
 #ifdef __cplusplus
 }
 #endif

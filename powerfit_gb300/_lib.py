@@ -25,6 +25,7 @@ EXPORTS = [
     "pf_scan_resident", "pf_get_results", "pf_synchronize", "pf_set_stream", "pf_set_tuning", "pf_get_tuning", "pf_autotune",
     "pf_get_geometry", "pf_set_profiling", "pf_get_kernel_times", "pf_fft3d",
     "pf_rotate_grid3d", "pf_conj_multiply", "pf_calc_lcc", "pf_combine",
+    "pf_blur_points", "pf_dilate_points", "pf_laplace_wrap", "pf_core_indices", "pf_prep_error",
 ]
 
 
@@ -91,6 +92,11 @@ def load(path=None):
             "pf_conj_multiply": (_i, [_vp, _vp, _vp, _i64]),
             "pf_calc_lcc": (_i, [_vp, _vp, _vp, _vp, _vp, _i64]),
             "pf_combine": (_i, [_vp, _vp, _vp, _vp, _i64, _i64]),
+            "pf_blur_points": (_i, [_vp, _vp, _i64, _d, _vp, _i, _i, _i, _i]),
+            "pf_dilate_points": (_i, [_vp, _vp, _i64, _vp, _i, _i, _i, _i]),
+            "pf_laplace_wrap": (_i, [_vp, _vp, _i, _i, _i]),
+            "pf_core_indices": (_i, [_vp, _vp, _i, _i, _i]),
+            "pf_prep_error": (_i, [ctypes.c_char_p, _sz]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -280,3 +286,60 @@ def combine_into(lcc, rot, part_lcc, part_rot, rot_add):
         raise ValueError("combine: dtype/size mismatch")
     check(load().pf_combine(ptr(lcc), ptr(rot), ptr(pl), ptr(pr), lcc.size, int(rot_add)))
     return lcc, rot
+
+
+# ---- preprocessing on the GPU ---------------------------------------------
+
+def _check_prep(rc):
+    if rc != 0:
+        buf = ctypes.create_string_buffer(256)
+        load().pf_prep_error(buf, 256)
+        raise PowerFitError(rc, buf.value.decode(errors="replace"))
+
+
+def _grid_out(out):
+    if out.dtype != np.float64 or not out.flags.c_contiguous or out.ndim != 3:
+        raise ValueError("out must be a C-contiguous 3D float64 array")
+    return out.shape
+
+
+def blur_points(points, weights, sigma, out, wraparound=True):
+    """GPU mirror of ``_powerfit.blur_points`` (adds into ``out``)."""
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(3, -1)
+    w = np.ascontiguousarray(weights, dtype=np.float64).reshape(-1)
+    if w.size != pts.shape[1]:
+        raise ValueError("weights array is of incorrect size")
+    nz, ny, nx = _grid_out(out)
+    _check_prep(load().pf_blur_points(ptr(pts), ptr(w), pts.shape[1], float(sigma), ptr(out), nz, ny, nx,
+                                      int(bool(wraparound))))
+    return out
+
+
+def dilate_points(points, radii, out, wraparound=True):
+    """GPU mirror of ``_powerfit.dilate_points`` (sets balls to 1 in ``out``)."""
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(3, -1)
+    r = np.ascontiguousarray(np.broadcast_to(np.asarray(radii, dtype=np.float64), (pts.shape[1],)))
+    nz, ny, nx = _grid_out(out)
+    _check_prep(load().pf_dilate_points(ptr(pts), ptr(r), pts.shape[1], ptr(out), nz, ny, nx,
+                                        int(bool(wraparound))))
+    return out
+
+
+def laplace_wrap(array):
+    """GPU ``scipy.ndimage.laplace(array, mode='wrap')`` (float64)."""
+    a = c64(array)
+    if a.ndim != 3:
+        raise ValueError("laplace_wrap expects a 3D array")
+    out = np.empty_like(a)
+    _check_prep(load().pf_laplace_wrap(ptr(a), ptr(out), *a.shape))
+    return out
+
+
+def core_indices(mask):
+    """GPU ``determine_core_indices``: erosions survived per voxel (float64)."""
+    m = c64(mask)
+    if m.ndim != 3:
+        raise ValueError("core_indices expects a 3D array")
+    out = np.empty_like(m)
+    _check_prep(load().pf_core_indices(ptr(m), ptr(out), *m.shape))
+    return out

@@ -118,6 +118,11 @@ class CUDACorrelator(BaseCorrelator):
         ftarget = self._laplace_filter(self._target) if self._laplace else self._target
         self._ctx.set_target(ftarget, self._lcc_mask)
 
+    @staticmethod
+    def _laplace_filter(array):
+        """Periodic Laplace filter on the GPU (``pf_laplace_wrap``)."""
+        return _lib.laplace_wrap(array)
+
     @BaseCorrelator.mask.setter
     def mask(self, mask):
         BaseCorrelator.mask.fset(self, mask)

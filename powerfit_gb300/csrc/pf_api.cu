@@ -120,6 +120,7 @@ struct pf_ctx {
   int pairs = 1, ty1 = 16, ty3 = 16;
   size_t max_smem = 0;
   bool fast = false;                 // compile-time-specialised kernels for this grid
+  bool split = false;                // (z, y) plane larger than shared memory: pass 2 in three steps
   FastLaunch fl{};
   bool profiling = false;
   double ms[3] = {0, 0, 0};
@@ -276,6 +277,8 @@ int set_smem_limits(pf_ctx* c) {
   PF_CUDA(c, allow_smem(k_pass3, m));
   PF_CUDA(c, allow_smem(k_fwd_x_real, m));
   PF_CUDA(c, allow_smem(k_pass2, m));
+  PF_CUDA(c, allow_smem(k_split_rows, m));
+  PF_CUDA(c, allow_smem(k_split_cols, m));
   if (c->fast) PF_CUDA(c, c->fl.set_attrs(m, m));
   return PF_OK;
 }
@@ -326,6 +329,30 @@ int upload_double_as_float(pf_ctx* c, float* dst, const double* src, long long n
   return PF_OK;
 }
 
+constexpr int kSplitRows = 16;   // rows per tile of the split pass 2 (steps 2a, 2c)
+constexpr int kSplitCols = 16;   // columns per tile (step 2b)
+
+// pass 2 in three steps through global memory (planes larger than shared memory)
+int launch_split_pass2(pf_ctx* c, const Geometry& g, int npairs, int nfield, int mode, float2* out, float scale) {
+  const size_t srow = ((size_t)c->ny + (size_t)kSplitRows * (c->ny + kPad)) * sizeof(float2);
+  const size_t scol = ((size_t)c->nz + (size_t)c->nz * (kSplitCols + kPad)) * sizeof(float2);
+  SplitRowsParams pr{g, c->py, c->twy, c->buf, nfield, kSplitRows, 0};
+  dim3 gr((g.nvz + kSplitRows - 1) / kSplitRows, c->nx, npairs * nfield);
+  k_split_rows<<<gr, kThreadsLine, srow, c->stream>>>(pr);
+  PF_CUDA(c, cudaGetLastError());
+  SplitColsParams pc{g, c->pz, c->twz, c->buf, c->spec, c->spec + c->N, nfield, kSplitCols, mode, out, scale};
+  dim3 gc((c->ny + kSplitCols - 1) / kSplitCols, c->nx, npairs * nfield);
+  k_split_cols<<<gc, kThreadsLine, scol, c->stream>>>(pc);
+  PF_CUDA(c, cudaGetLastError());
+  if (mode == 0) {
+    SplitRowsParams pi{g, c->py, c->twy, c->buf, nfield, kSplitRows, 1};
+    dim3 gi((c->nz + kSplitRows - 1) / kSplitRows, c->nx, npairs * nfield);
+    k_split_rows<<<gi, kThreadsLine, srow, c->stream>>>(pi);
+    PF_CUDA(c, cudaGetLastError());
+  }
+  return PF_OK;
+}
+
 // forward transforms of two real device fields -> spectra [2][kx][kz][ky] * scale
 int forward_two_fields(pf_ctx* c, const float* in0, const float* in1, int square1, float2* out, float scale) {
   int rc = ensure_buf(c, 1);
@@ -350,8 +377,14 @@ int forward_two_fields(pf_ctx* c, const float* in0, const float* in1, int square
   p2.out = out;
   p2.scale = scale;
   dim3 g2(c->nx, 2, 1);
-  if (c->fast) c->fl.pass2(p2, 0, g2, plane_smem(c->ny, c->nz), c->stream);
-  else k_pass2<<<g2, kThreadsPlane, plane_smem(c->ny, c->nz), c->stream>>>(p2);
+  if (c->split) {
+    int rc2 = launch_split_pass2(c, gfull, 1, 2, 1, out, scale);
+    if (rc2) return rc2;
+  } else if (c->fast) {
+    c->fl.pass2(p2, 0, g2, plane_smem(c->ny, c->nz), c->stream);
+  } else {
+    k_pass2<<<g2, kThreadsPlane, plane_smem(c->ny, c->nz), c->stream>>>(p2);
+  }
   PF_CUDA(c, cudaGetLastError());
   PF_CUDA(c, cudaStreamSynchronize(c->stream));
   return PF_OK;
@@ -407,14 +440,9 @@ pf_ctx* pf_create(int nz, int ny, int nx, int device, int* status) {
   cudaDeviceProp prop;
   cudaGetDeviceProperties(&prop, device);
   c->max_smem = prop.sharedMemPerBlockOptin;
-  if (plane_smem(ny, nz) > c->max_smem) {
-    set_global_error("grid (%d, %d, %d): a (z, y) plane needs %zu bytes of shared memory, the device offers %zu",
-                     nz, ny, nx, plane_smem(ny, nz), c->max_smem);
-    delete c;
-    return ret(PF_E_SHAPE);
-  }
+  c->split = plane_smem(ny, nz) > c->max_smem;
   c->rmax = std::min(nz, std::min(ny, nx)) / 2;
-  if (nz == ny && ny == nx) c->fast = fast_table(nx, &c->fl);
+  if (nz == ny && ny == nx && !c->split) c->fast = fast_table(nx, &c->fl);
   choose_tiles(c);
   int rc = PF_OK;
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
@@ -633,7 +661,8 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     p2.mode = 0;
     dim3 g2(c->nx, 3, npairs);
     rc = timed_launch(c, 1, [&] {
-      if (fast) c->fl.pass2(p2, re2, g2, s2, c->stream);
+      if (c->split) launch_split_pass2(c, g, npairs, 3, 0, nullptr, 1.0f);
+      else if (fast) c->fl.pass2(p2, re2, g2, s2, c->stream);
       else k_pass2<<<g2, kThreadsPlane, s2, c->stream>>>(p2);
     });
     if (rc) return rc;

@@ -306,6 +306,114 @@ __global__ void __launch_bounds__(kThreadsPlane) k_pass2(const Pass2Params p) {
 #endif  // PF_GENERIC_KERNELS
 
 // ---------------------------------------------------------------------------
+// Pass 2, split form for (z, y) planes larger than shared memory (e.g. 192^3):
+//   2a  y transforms of tiles of rows (forward: valid planes only),
+//   2b  per tile of y columns: z forward, conj product (or forward only),
+//       z inverse,
+//   2c  inverse y transforms of tiles of rows.
+// The planes go through global memory between the steps.
+// ---------------------------------------------------------------------------
+struct SplitRowsParams {
+  Geometry g;
+  AxisPlan py;
+  const float2* __restrict__ twy;
+  float2* __restrict__ buf;
+  int nfield;
+  int rows_per_tile;
+  int inverse;     // 0: forward, valid z rows only; 1: inverse, all rows
+};
+
+struct SplitColsParams {
+  Geometry g;
+  AxisPlan pz;
+  const float2* __restrict__ twz;
+  float2* __restrict__ buf;
+  const float2* __restrict__ s1;
+  const float2* __restrict__ s2;
+  int nfield;
+  int cols_per_tile;
+  int mode;                       // 0: z forward, product, z inverse; 1: z forward only -> out
+  float2* __restrict__ out;
+  float scale;
+};
+
+#ifdef PF_GENERIC_KERNELS
+// grid: (row tiles of one (field, kx) plane, kx, pair * nfield + field)
+__global__ void __launch_bounds__(kThreadsLine) k_split_rows(const SplitRowsParams p) {
+  extern __shared__ float2 sm[];
+  const Geometry& g = p.g;
+  const int Y = g.ny, Z = g.nz;
+  float2* tw = sm;
+  float2* t = sm + Y;                           // [rows][Y + kPad]
+  const int rs = Y + kPad;
+  for (int i = threadIdx.x; i < Y; i += blockDim.x) tw[i] = p.twy[i];
+  const int nrow_all = p.inverse ? Z : g.nvz;
+  const int r0 = blockIdx.x * p.rows_per_tile;
+  const int nr = min(p.rows_per_tile, nrow_all - r0);
+  if (nr <= 0) return;
+  const int kx = blockIdx.y;
+  float2* gplane = p.buf + ((long long)blockIdx.z * g.nx + kx) * ((long long)Z * Y);
+  auto row_of = [&](int l) { const int i = r0 + l; return (p.inverse || i <= g.zlo) ? i : i + Z - g.nvz; };
+  for (int v = threadIdx.x; v < nr * Y; v += blockDim.x) {
+    const int l = v / Y, y = v - l * Y;
+    t[l * rs + y] = gplane[(long long)row_of(l) * Y + y];
+  }
+  __syncthreads();
+  SmemLines lines{t, rs, 1};
+  if (p.inverse) fft_lines<true, kEmax>(p.py, nr, tw, lines, lines, lines, true, true);
+  else fft_lines<false, kEmax>(p.py, nr, tw, lines, lines, lines, true, true);
+  for (int v = threadIdx.x; v < nr * Y; v += blockDim.x) {
+    const int l = v / Y, y = v - l * Y;
+    gplane[(long long)row_of(l) * Y + y] = t[l * rs + y];
+  }
+}
+
+// grid: (column tiles, kx, pair * nfield + field)
+__global__ void __launch_bounds__(kThreadsLine) k_split_cols(const SplitColsParams p) {
+  extern __shared__ float2 sm[];
+  const Geometry& g = p.g;
+  const int Y = g.ny, Z = g.nz;
+  const int TC = p.cols_per_tile;
+  float2* tw = sm;
+  float2* t = sm + Z;                           // [Z][TC + kPad]
+  const int rs = TC + kPad;
+  for (int i = threadIdx.x; i < Z; i += blockDim.x) tw[i] = p.twz[i];
+  const int y0 = blockIdx.x * TC;
+  const int nc = min(TC, Y - y0);
+  const int kx = blockIdx.y;
+  const int pf = blockIdx.z;
+  const int f = pf % p.nfield;
+  const long long plane = (long long)Z * Y;
+  float2* gplane = p.buf + ((long long)pf * g.nx + kx) * plane;
+  const int nvz = g.nvz;
+  for (int v = threadIdx.x; v < Z * TC; v += blockDim.x) {
+    const int z = v / TC, c = v - z * TC;
+    const bool valid = c < nc && (p.mode == 1 || z <= g.zlo || z >= Z - (nvz - g.zlo - 1));
+    t[z * rs + c] = valid ? gplane[(long long)z * Y + y0 + c] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  SmemLines cols{t, 1, rs};
+  if (p.mode == 0) {
+    const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + (long long)kx * plane + y0;
+    ProductStore prod{t, rs, spec, Y};
+    fft_lines<false, kEmax>(p.pz, nc, tw, cols, cols, prod, true, true);
+    fft_lines<true, kEmax>(p.pz, nc, tw, cols, cols, cols, true, true);
+    for (int v = threadIdx.x; v < Z * TC; v += blockDim.x) {
+      const int z = v / TC, c = v - z * TC;
+      if (c < nc) gplane[(long long)z * Y + y0 + c] = t[z * rs + c];
+    }
+  } else {
+    fft_lines<false, kEmax>(p.pz, nc, tw, cols, cols, cols, true, true);
+    float2* o = p.out + ((long long)f * g.nx + kx) * plane;
+    for (int v = threadIdx.x; v < Z * TC; v += blockDim.x) {
+      const int z = v / TC, c = v - z * TC;
+      if (c < nc) o[(long long)z * Y + y0 + c] = cscale(t[z * rs + c], p.scale);
+    }
+  }
+}
+#endif  // PF_GENERIC_KERNELS
+
+// ---------------------------------------------------------------------------
 // Pass 3: inverse x transform, LCC, running max / argmax
 // ---------------------------------------------------------------------------
 struct Pass3Params {

@@ -1,7 +1,7 @@
 """Generate the golden fixtures from the real reference (run in a container that
 has the reference tree at /root/reference; the fixtures are committed).
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [prep]   (``prep``: only prep.npz, ref_map.mrc, analyzer.npz)
 
 Each fixture records reference outputs for seeded inputs:
 
@@ -9,6 +9,11 @@ Each fixture records reference outputs for seeded inputs:
   grid of the reference's ``tests/test_extensions.py`` recipe plus random grids,
   random rotations, both interpolation modes and several radii.
 * ``lcc_helpers.npz``: ``_powerfit.conj_multiply`` and ``_powerfit.calc_lcc``.
+* ``prep.npz``: ``_powerfit.blur_points`` / ``dilate_points`` (template and
+  mask builders), ``BaseCorrelator._laplace_filter`` and
+  ``helpers.determine_core_indices`` on seeded inputs.
+* ``ref_map.mrc``: a map written by the reference's ``volume.to_mrc``;
+  ``analyzer.npz``: the reference ``Analyzer``'s solutions on seeded peaks.
 * ``scan_<name>.npz``: ``CPUCorrelator`` (numpy.fft path) full scans:
   inputs (float32-exact), rotations, best LCC, best rotation and, from the
   oracle restatement (checked equal to the reference first), the per-voxel
@@ -91,6 +96,54 @@ def gen_helpers(pf):
                         gcc=gcc, ave=ave, ave2=ave2, mask=mask, lcc=lcc)
 
 
+def gen_prep(pfx, powerfitter, helpers):
+    rng = np.random.default_rng(31)
+    out = {}
+    shape = (20, 22, 24)
+    pts = rng.random((3, 60)) * np.array([[24.0], [22.0], [20.0]]) - 4.0
+    w = rng.random(60) + 0.5
+    for wrap in (True, False):
+        a = np.zeros(shape)
+        pfx.blur_points(pts.copy(), w.copy(), 1.3, a, wrap)
+        out["blur_%d" % wrap] = a
+        b = np.zeros(shape)
+        radii = 1.0 + 2.0 * rng.random(60)
+        pfx.dilate_points(pts.copy(), radii.copy(), b, wrap)
+        out["dilate_%d" % wrap] = b
+        out["radii_%d" % wrap] = radii
+    out["points"] = pts
+    out["weights"] = w
+    grid = rng.random((9, 10, 11))
+    out["lap_in"] = grid
+    out["lap_out"] = powerfitter.BaseCorrelator._laplace_filter(grid)
+    blob = np.zeros((16, 18, 20))
+    blob[2:14, 3:15, 1:19] = 1
+    blob[5:9, 0:18, 8:12] = 1
+    blob[0, 0, 0] = 1
+    out["core_in"] = blob
+    out["core_out"] = helpers.determine_core_indices(blob)
+    np.savez_compressed(os.path.join(HERE, "prep.npz"), **out)
+
+
+def gen_io(volume_mod, analyzer_mod):
+    rng = np.random.default_rng(41)
+    arr = rng.random((10, 12, 14)).astype(np.float32).astype(np.float64)
+    vol = volume_mod.Volume(arr, 1.5, np.array([3.0, -2.0, 5.0]))
+    volume_mod.to_mrc(os.path.join(HERE, "ref_map.mrc"), vol)
+    # analyzer: a few smooth peaks on a 24^3 grid
+    shape = (24, 24, 24)
+    lcc = np.zeros(shape)
+    zz, yy, xx = np.meshgrid(*[np.arange(n) for n in shape], indexing="ij")
+    for c, h in zip(rng.random((5, 3)) * 20 + 2, rng.random(5) * 0.5 + 0.3):
+        lcc = np.maximum(lcc, h * np.exp(-((zz - c[0]) ** 2 + (yy - c[1]) ** 2 + (xx - c[2]) ** 2) / 6.0))
+    rot_ind = rng.integers(0, 7, shape).astype(np.float64)
+    rotmats = quat_to_rotmat(rng.normal(size=(7, 4)))
+    an = analyzer_mod.Analyzer(lcc, rotmats, rot_ind, voxelspacing=1.7, origin=(1.0, 2.0, 3.0), z_sigma=0.12)
+    sols = np.array(an.solutions)
+    np.savez_compressed(os.path.join(HERE, "analyzer.npz"), lcc=lcc, rot_ind=rot_ind, rotmats=rotmats,
+                        solutions=sols)
+
+
 def random_case(shape, seed):
     rng = np.random.default_rng(seed)
     target = f32(rng.random(shape))
@@ -142,6 +195,10 @@ def main():
     powerfitter = refimport.module("powerfitter")
     helpers = refimport.module("helpers")
     rot = refimport.module("rotations")
+    gen_prep(pfx, powerfitter, helpers)
+    gen_io(refimport.module("volume"), refimport.module("analyzer"))
+    if len(sys.argv) > 1 and sys.argv[1] == "prep":
+        return
     gen_rotate(ext, rot)
     gen_helpers(pfx)
 

@@ -262,3 +262,21 @@ def test_autotune_keeps_results(lib):
     assert cfg["rows3"] & (cfg["rows3"] - 1) == 0
     lcc, r = ctx.scan(rot)
     assert np.array_equal(lcc, base.lcc) and np.array_equal(r, base.rot)
+
+
+def test_split_plane_path_vs_oracle(lib):
+    """(z, y) planes larger than shared memory take the three-step pass 2."""
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    from powerfit_gb300 import synth
+    shape = (192, 192, 12)
+    c = synth.make_case(shape, 2.0, 300, 2, 8.0, 5.0, 21)
+    rot = quat_to_rotmat(super_fibonacci(60))[::12]
+    target = c.target.astype(np.float64)
+    corr = correlator(target, c.template, c.mask, rot, False)
+    p = O.prepare(target, c.template, c.mask, False)
+    lcc, rrot, second = O.scan(p, rot, track_second=True)
+    check_parity(corr.lcc, corr.rot, lcc, rrot, second, "split 192x192x12")
+    a = np.random.default_rng(2).standard_normal((192, 160, 8)).astype(np.float32)
+    out = lib.Context(a.shape).fft3d(a)
+    ref = np.fft.fftn(a.astype(np.float64))
+    assert np.max(np.abs(out - ref)) / np.max(np.abs(ref)) < 2e-6

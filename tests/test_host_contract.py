@@ -174,3 +174,15 @@ def test_library_exports_every_header_symbol():
         assert hasattr(lib, s), s
     from powerfit_gb300 import _lib
     assert sorted(_lib.EXPORTS) == syms
+
+
+def test_host_splat_matches_reference_outputs():
+    d = np.load(os.path.join(ROOT, "tests", "golden", "prep.npz"))
+    for wrap in (1, 0):
+        a = np.zeros(d["blur_%d" % wrap].shape)
+        synth.blur_points(d["points"], d["weights"], 1.3, a, bool(wrap))
+        assert np.max(np.abs(a - d["blur_%d" % wrap])) < 1e-12
+        b = np.zeros(a.shape)
+        synth.dilate_points(d["points"], d["radii_%d" % wrap], b, bool(wrap))
+        assert np.array_equal(b, d["dilate_%d" % wrap])
+    assert np.array_equal(determine_core_indices(d["core_in"]), d["core_out"])
