@@ -50,6 +50,28 @@ def fisher_sigma(mv, fsc):
 
 
 def main(argv=None):
+    t0 = time()
+    args = parse_args(argv)
+    os.makedirs(args.directory, exist_ok=True)
+    log = logging.getLogger("powerfit_gb300.cli")
+    log.setLevel(logging.INFO)
+    handler = logging.FileHandler(os.path.join(args.directory, "powerfit.log"))
+    handler.setFormatter(logging.Formatter("%(asctime)s %(message)s"))
+    log.addHandler(handler)
+
+    def write(line):
+        if sys.stdout.isatty():
+            print(line)
+        log.info(line)
+
+    try:
+        return _run(args, write, t0)
+    finally:
+        log.removeHandler(handler)
+        handler.close()
+
+
+def _run(args, write, t0):
     from . import CUDACorrelator
     from .analyzer import Analyzer
     from ._lib import core_indices
@@ -57,18 +79,7 @@ def main(argv=None):
     from .structure import Structure, write_fits_to_pdb
     from .volume import Volume, extend, nearest_multiple2357, resample, structure_to_shape_like, trim
 
-    t0 = time()
-    args = parse_args(argv)
-    os.makedirs(args.directory, exist_ok=True)
-    logging.basicConfig(filename=os.path.join(args.directory, "powerfit.log"), level=logging.INFO,
-                        format="%(asctime)s %(message)s")
-
-    def write(line):
-        if sys.stdout.isatty():
-            print(line)
-        logging.info(line)
-
-    logging.info(" ".join(sys.argv))
+    write(" ".join(sys.argv))
     target = Volume.fromfile(args.target)
     write("Target resolution: {:.2f}".format(args.resolution))
     if not args.no_resampling:
