@@ -26,6 +26,7 @@ EXPORTS = [
     "pf_get_geometry", "pf_set_profiling", "pf_get_kernel_times", "pf_fft3d",
     "pf_rotate_grid3d", "pf_conj_multiply", "pf_calc_lcc", "pf_combine",
     "pf_blur_points", "pf_dilate_points", "pf_laplace_wrap", "pf_core_indices", "pf_prep_error",
+    "pf_scan_noalloc",
 ]
 
 
@@ -97,6 +98,7 @@ def load(path=None):
             "pf_laplace_wrap": (_i, [_vp, _vp, _i, _i, _i]),
             "pf_core_indices": (_i, [_vp, _vp, _i, _i, _i]),
             "pf_prep_error": (_i, [ctypes.c_char_p, _sz]),
+            "pf_scan_noalloc": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _d, _i, _vp, _i64, _i64, _vp, _vp, _vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)

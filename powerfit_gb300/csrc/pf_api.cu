@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <functional>
+#include <mutex>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -881,6 +882,192 @@ int pf_fft3d(pf_ctx* c, const float* in, float* out) {
   if (din) cudaFree(din);
   if (dout) cudaFree(dout);
   return rc;
+}
+
+// ------------------------- scan without device allocation ------------------
+//
+// For callers that cannot allocate device memory while they run (a host that
+// hands all device memory to its own allocator at start-up and forbids any
+// later cudaMalloc, or a plugin that may only use the buffers its host gives
+// it).  Every intermediate array of the search lives in one file-scope device
+// array of fixed size instead of memory allocated per call.
+namespace {
+
+// Largest grid: N = nz*ny*nx <= kNoAllocMaxVoxels (64^3), edges <= 256.
+constexpr long long kNoAllocMaxVoxels = 64LL * 64 * 64;
+constexpr int kNoAllocMaxEdge = 256;
+constexpr int kNoAllocRotChunk = 1024;                       // rotations converted per chunk
+constexpr size_t kNoAllocSpecBytes = 2ull * kNoAllocMaxVoxels * sizeof(float2);   // target spectra
+constexpr size_t kNoAllocBufBytes = 3ull * kNoAllocMaxVoxels * sizeof(float2);    // one rotation pair
+constexpr size_t kNoAllocTwBytes = 3ull * kNoAllocMaxEdge * sizeof(float2);
+constexpr size_t kNoAllocRotBytes = (size_t)kNoAllocRotChunk * sizeof(RotFixed);
+constexpr size_t kNoAllocBytes = kNoAllocSpecBytes + kNoAllocBufBytes + kNoAllocTwBytes + kNoAllocRotBytes;
+
+// The scratch itself (about 10.1 MiB), held by every GPU that loads the
+// library until the process exits.  Host code must not use the symbol as an
+// address: the device address comes from cudaGetSymbolAddress below.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+unsigned char* g_noalloc_addr[kNoAllocMaxDevices] = {};
+std::mutex g_noalloc_mutex;
+
+// device address of the scratch on the current device (set up on first use)
+int noalloc_scratch(unsigned char** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
+    return fail(nullptr, PF_E_CUDA, "pf_scan_noalloc: no current CUDA device");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+      return fail(nullptr, PF_E_CUDA, "pf_scan_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+    g_noalloc_addr[dev] = (unsigned char*)ptr;
+  }
+  *out = g_noalloc_addr[dev];
+  return PF_OK;
+}
+
+__global__ void k_rot_to_fixed(const double* __restrict__ rd, long long n, RotFixed* __restrict__ out) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) {
+    RotFixed f;
+    for (int k = 0; k < 9; ++k) f.r[k] = llround(rd[9 * i + k] * 4294967296.0);
+    out[i] = f;
+  }
+}
+
+}  // namespace
+
+int pf_scan_noalloc(int nz, int ny, int nx, const float* d_target, const uint8_t* d_lcc_mask, const float* d_tmpl,
+                    const float* d_mask, double norm_factor, int rmax, const double* d_rotmats, int64_t nrot,
+                    int64_t rot_offset, float* d_lcc, int32_t* d_rot, void* stream) {
+  if (nz < 1 || ny < 1 || nx < 1 || nz > kNoAllocMaxEdge || ny > kNoAllocMaxEdge || nx > kNoAllocMaxEdge ||
+      (long long)nz * ny * nx > kNoAllocMaxVoxels)
+    return fail(nullptr, PF_E_SHAPE,
+                "pf_scan_noalloc: grid (%d, %d, %d) exceeds the fixed scratch (at most %lld voxels, edges <= %d)",
+                nz, ny, nx, kNoAllocMaxVoxels, kNoAllocMaxEdge);
+  if (!d_target || !d_lcc_mask || !d_tmpl || !d_mask || !d_lcc || !d_rot || (!d_rotmats && nrot > 0) || nrot < 0)
+    return fail(nullptr, PF_E_ARG, "pf_scan_noalloc: null pointer or negative rotation count");
+  if (!(norm_factor > 0)) return fail(nullptr, PF_E_ARG, "pf_scan_noalloc: norm_factor must be positive");
+  if (rmax < 0 || 2 * rmax > std::min(nz, std::min(ny, nx)))
+    return fail(nullptr, PF_E_ARG, "pf_scan_noalloc: rmax %d outside [0, min(shape)//2]", rmax);
+  if (rot_offset < 0 || rot_offset + nrot > (int64_t)0x7fffffff)
+    return fail(nullptr, PF_E_ARG, "pf_scan_noalloc: rotation index overflows int32");
+  // plans from the constexpr planner (no host allocation either)
+  auto plan_of = [](int n, AxisPlan* pl) {
+    const CtPlan c = ct_plan(n);
+    if (c.nst < 1) return false;
+    int prod = 1;
+    for (int i = 0; i < c.nst; ++i) prod *= c.r[i];
+    if (prod != n) return false;
+    pl->n = n;
+    pl->nst = c.nst;
+    for (int i = 0; i < c.nst; ++i) pl->radix[i] = c.r[i];
+    return true;
+  };
+  AxisPlan px, py, pz;
+  if (!plan_of(nx, &px) || !plan_of(ny, &py) || !plan_of(nz, &pz))
+    return fail(nullptr, PF_E_SHAPE, "pf_scan_noalloc: every edge must factor into 2, 3, 5 and 7");
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return fail(nullptr, PF_E_CUDA, "no device properties");
+  if (plane_smem(ny, nz) > prop.sharedMemPerBlockOptin)
+    return fail(nullptr, PF_E_SHAPE, "pf_scan_noalloc: the (z, y) plane does not fit in shared memory");
+  unsigned char* scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long N = (long long)nz * ny * nx;
+  float2* spec = (float2*)scratch;
+  float2* buf = (float2*)(scratch + kNoAllocSpecBytes);
+  float2* twx = (float2*)(scratch + kNoAllocSpecBytes + kNoAllocBufBytes);
+  float2* twy = twx + kNoAllocMaxEdge;
+  float2* twz = twy + kNoAllocMaxEdge;
+  RotFixed* rots = (RotFixed*)(scratch + kNoAllocSpecBytes + kNoAllocBufBytes + kNoAllocTwBytes);
+
+  // kernel attributes (idempotent) and twiddles (host tables, as for contexts)
+  const size_t m = prop.sharedMemPerBlockOptin;
+  PF_CUDA(nullptr, allow_smem(k_pass1, m));
+  PF_CUDA(nullptr, allow_smem(k_pass2, m));
+  PF_CUDA(nullptr, allow_smem(k_pass3, m));
+  PF_CUDA(nullptr, allow_smem(k_fwd_x_real, m));
+  float2 tw_host[3][kNoAllocMaxEdge];   // same tables as the contexts build (twiddles())
+  const int edges[3] = {nx, ny, nz};
+  for (int a = 0; a < 3; ++a)
+    for (int mm = 0; mm < edges[a]; ++mm) {
+      const double ang = 2.0 * M_PI * (double)mm / (double)edges[a];
+      tw_host[a][mm] = make_float2((float)std::cos(ang), (float)-std::sin(ang));
+    }
+  // pageable source: the copies are staged before the calls return
+  PF_CUDA(nullptr, cudaMemcpyAsync(twx, tw_host[0], nx * sizeof(float2), cudaMemcpyHostToDevice, s));
+  PF_CUDA(nullptr, cudaMemcpyAsync(twy, tw_host[1], ny * sizeof(float2), cudaMemcpyHostToDevice, s));
+  PF_CUDA(nullptr, cudaMemcpyAsync(twz, tw_host[2], nz * sizeof(float2), cudaMemcpyHostToDevice, s));
+
+  // target spectra FT(target)/N and FT(target^2)/N into the scratch
+  Geometry g{};
+  g.nz = nz;
+  g.ny = ny;
+  g.nx = nx;
+  g.rmax = rmax;
+  g.reff = rmax;
+  g.nvz = nz;
+  g.zlo = nz - 1;
+  int ty1 = 16;
+  while (ty1 > 1 && ((long long)ty1 * nx > (long long)kMaxVoxPerThread * kThreadsLine || line_smem(nx, 3, ty1) > 96 * 1024))
+    ty1--;
+  int ty3 = 16;
+  while (ty3 > 1 && (long long)ty3 * nx > (long long)kMaxVoxPerThread * kThreadsLine) ty3 /= 2;
+  FwdXParams fx{g, px, twx, d_target, nullptr, 1, buf, ty1};
+  k_fwd_x_real<<<dim3(nz, (ny + ty1 - 1) / ty1, 1), kThreadsLine, line_smem(nx, 3, ty1), s>>>(fx);
+  PF_CUDA(nullptr, cudaGetLastError());
+  Pass2Params pt{};
+  pt.g = g;
+  pt.py = py;
+  pt.pz = pz;
+  pt.twy = twy;
+  pt.twz = twz;
+  pt.buf = buf;
+  pt.nfield = 2;
+  pt.mode = 1;
+  pt.out = spec;
+  pt.scale = (float)(1.0 / (double)N);
+  k_pass2<<<dim3(nx, 2, 1), kThreadsPlane, plane_smem(ny, nz), s>>>(pt);
+  PF_CUDA(nullptr, cudaGetLastError());
+
+  // the outputs start at zero (strict > against 0, rotation 0)
+  PF_CUDA(nullptr, cudaMemsetAsync(d_lcc, 0, N * sizeof(float), s));
+  PF_CUDA(nullptr, cudaMemsetAsync(d_rot, 0, N * sizeof(int32_t), s));
+
+  // one rotation pair per pass: buf holds exactly one pair
+  for (int64_t c0 = 0; c0 < nrot; c0 += kNoAllocRotChunk) {
+    const int64_t cn = std::min<int64_t>(kNoAllocRotChunk, nrot - c0);
+    k_rot_to_fixed<<<(unsigned)((cn + 127) / 128), 128, 0, s>>>(d_rotmats + 9 * c0, cn, rots);
+    PF_CUDA(nullptr, cudaGetLastError());
+    for (int64_t r0 = 0; r0 < cn; r0 += 2) {
+      Pass1Params p1{g, px, GatherSrc{d_tmpl, d_mask}, twx, rots, d_rotmats + 9 * c0, r0, cn, buf, ty1, nullptr, 0};
+      k_pass1<<<dim3(nz, (ny + ty1 - 1) / ty1, 1), kThreadsLine, line_smem(nx, 3, ty1), s>>>(p1);
+      Pass2Params p2{};
+      p2.g = g;
+      p2.py = py;
+      p2.pz = pz;
+      p2.twy = twy;
+      p2.twz = twz;
+      p2.buf = buf;
+      p2.s1 = spec;
+      p2.s2 = spec + N;
+      p2.nfield = 3;
+      p2.mode = 0;
+      k_pass2<<<dim3(nx, 3, 1), kThreadsPlane, plane_smem(ny, nz), s>>>(p2);
+      Pass3Params p3{g, px, twx, buf, 1, r0, cn, rot_offset + c0, d_lcc_mask, (float)norm_factor,
+                     d_lcc, d_rot, ty3, 0};
+      k_pass3<<<dim3(nz, (ny + ty3 - 1) / ty3, 1), kThreadsLine, line_smem(nx, 3, ty3), s>>>(p3);
+      PF_CUDA(nullptr, cudaGetLastError());
+    }
+  }
+  return PF_OK;
 }
 
 // ----------------------------- unit-level mirrors ---------------------------
