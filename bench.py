@@ -34,6 +34,11 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 METRIC = "rotations/s at 128^3 LCC (1 GB300)"
+
+
+def metric_for(shape):
+    return "rotations/s at %d^3 LCC (1 GB300)" % shape[0] if len(set(shape)) == 1 else \
+        "rotations/s at %dx%dx%d LCC (1 GB300)" % tuple(shape)
 UNIT = "rotations/s"
 
 
@@ -49,6 +54,9 @@ def parse():
     ap.add_argument("--cpu-rot-per-core", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--pairs", type=int, default=0)
+    ap.add_argument("--precision", action="store_true",
+                    help="precision study: GPU variants vs the float64 oracle on a rotation subset")
+    ap.add_argument("--precision-rotations", type=int, default=32)
     return ap.parse_args()
 
 
@@ -163,7 +171,7 @@ def run_reference(args, rank, world):
     pool.close()
     value = tot_rot / tot_t
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "impl": "reference", "metric": metric_for(target.shape), "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded map, template, mask; %s)" % desc,
@@ -347,11 +355,11 @@ def run_ours(args, rank, world, local_rank):
     pipe_bytes = bytes_per_rotation(n, 2 * pairs)
     pruned_bytes = sum(per_pair.values()) / 2.0
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": metric_for(shape), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 FFT / float-float LCC",
         "data": "synthetic (seeded map, template, mask; %s)" % desc,
-        "config": {"workload": args.config, "grid": list(shape), "voxelspacing": 1.5,
+        "config": {"workload": args.config, "grid": list(shape), "voxelspacing": cfg["voxelspacing"],
                    "laplace": cfg["laplace"], "core_weighted": cfg["core_weighted"],
                    "rotation_set_size": nset, "rotations_per_step": per_step,
                    "pairs_per_batch": pairs, "rows_pass1": ty1, "rows_pass3": ty3, "tuning": tuned,
@@ -388,8 +396,103 @@ def run_ours(args, rank, world, local_rank):
     return 0
 
 
+def run_queue(args):
+    """Uneven-map queue (16 seeded maps of 48^3-160^3, the 9.72 degree set's
+    size): all maps' scans queued on their own streams before any is awaited."""
+    import torch
+    from powerfit_gb300.queue import MapJob, make_queue, scan_queue
+    from powerfit_gb300.rotations import rotation_set
+    rot, desc = rotation_set(10.0, data_dir=os.environ.get("POWERFIT_ROTATION_DATA") or "/nonexistent")
+    if args.rotations:
+        rot = rot[:args.rotations]
+    cases = make_queue(16, seed=0)
+    mk = lambda: [MapJob(c.target.astype(np.float64), c.template, c.mask, rot, pairs=128) for c in cases]
+    for _ in range(max(1, args.warmup)):
+        scan_queue(mk(), autotune_trial=0)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        jobs = mk()
+        t0 = time.perf_counter()
+        scan_queue(jobs, autotune_trial=0)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    total_rot = rot.shape[0] * len(cases)
+    value = total_rot * len(times) / sum(times)
+    line = {"metric": "map-rotations/s, queue of 16 uneven maps (1 GB300)", "value": value,
+            "unit": "map-rotations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 FFT / float-float LCC", "data": "synthetic (%s)" % desc,
+            "config": {"workload": "queue16", "grids": [c.target.shape[0] for c in cases],
+                       "rotations_per_map": int(rot.shape[0]), "rotations_per_batch": 256,
+                       "timing": "host wall clock per step: per-map setup (spectra, template) + all scans"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_precision(args):
+    """Precision study: max |dLCC| and argmax agreement of the GPU variants
+    (float32 FFTs with float-float or float64 normalisation) against the
+    float64 oracle, on a rotation subset of the configuration."""
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    pool = mp.get_context("spawn").Pool(cores)
+    from powerfit_gb300 import CUDACorrelator, _lib
+    from oracle import oracle as O
+    cfg, target, template, mask, rot, desc = workload(args.config, args.rotations)
+    sub = rot[:: max(1, rot.shape[0] // args.precision_rotations)][:args.precision_rotations]
+    t0 = time.perf_counter()
+    # oracle with the top-two gap, one rotation slice per process (merged with _combine semantics)
+    per = -(-sub.shape[0] // cores)
+    jobs = [(target, template, mask, cfg["laplace"], sub[i:i + per]) for i in range(0, sub.shape[0], per)]
+    parts = pool.map(_oracle_top2, jobs)
+    pool.close()
+    lcc = np.zeros(target.shape)
+    second = np.zeros(target.shape)
+    rrot = np.zeros(target.shape)
+    for k, (pl, pr, ps) in enumerate(parts):
+        off = k * per
+        better = pl > lcc
+        with np.errstate(invalid="ignore"):
+            sec_new = np.where(better, np.maximum(lcc, ps), np.maximum(second, np.where(pl > second, pl, second)))
+        second = sec_new
+        lcc = np.where(better, pl, lcc)
+        rrot = np.where(better, pr + off, rrot)
+    oracle_s = time.perf_counter() - t0
+    res = {}
+    for name, flags in (("fp32_fft+floatfloat_norm", 0), ("fp32_fft+fp64_norm", _lib.PF_FLAG_FP64_NORM)):
+        corr = CUDACorrelator(target, laplace=cfg["laplace"], flags=flags)
+        corr.template = template
+        corr.mask = mask
+        corr.rotations = sub
+        corr.scan()
+        fin = np.isfinite(lcc)
+        err = float(np.max(np.abs(corr.lcc[fin] - lcc[fin])))
+        clear = fin & ((lcc - second) > 1e-4) & (lcc > 0)
+        agree = float(np.mean(corr.rot[clear] == rrot[clear])) if clear.any() else 1.0
+        res[name] = {"max_abs_dlcc": err, "argmax_agreement_where_gap_gt_1e-4": agree,
+                     "clear_voxels": int(clear.sum())}
+    line = {"metric": "precision vs float64 oracle", "config": {"workload": args.config, "grid": list(target.shape),
+            "rotations": int(sub.shape[0]), "laplace": cfg["laplace"], "core_weighted": cfg["core_weighted"]},
+            "variants": res, "oracle_s": oracle_s, "oracle_cores": cores,
+            "note": "a split-bf16x3 tensor-core DFT variant is not built (see DESIGN.md)"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _oracle_top2(job):
+    from oracle import oracle as O
+    target, template, mask, laplace, rots = job
+    p = O.prepare(target, template, mask, laplace)
+    return O.scan(p, rots, track_second=True)
+
+
 def main():
     args = parse()
+    if args.precision:
+        return run_precision(args)
+    if args.config == "queue16":
+        return run_queue(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -92,6 +92,11 @@ __device__ __forceinline__ void ct_stage(int nlines, const float2* __restrict__ 
   constexpr int C = ct_floor_pow2(C0 > 0 ? C0 : 1);
   constexpr int K = (C * NB + NT - 1) / NT;          // items per thread per chunk
   constexpr int TWMUL = L / (NS * R);
+  // The last stage (Ns * R == L) stores every item exactly where it loaded it
+  // (y[j + r Ns] with Ns == L/R), so no item can overwrite another's input:
+  // it needs no barrier between its loads and its stores.
+  constexpr bool kSelfInPlace = (NS * R == L);
+  if (kSelfInPlace) alias = false;
   for (int l0 = 0; l0 < nlines; l0 += C) {
     float2 v[K][R];
 #pragma unroll

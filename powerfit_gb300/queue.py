@@ -1,0 +1,97 @@
+"""Queue of maps of uneven size scanned together on one GPU.
+
+Each map gets its own context (its own compile-time- or runtime-planned
+kernels for its grid) on its own CUDA stream; after the per-map setup
+(target spectra, template, rotations), every map's scan is queued before any
+is awaited, so the kernels of small maps run beside those of large ones and
+fill the GPU together.  Results equal per-map scans (same kernels, same
+order of rotations per voxel).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from .correlator import BaseCorrelator
+
+
+class _Prep(BaseCorrelator):
+    """Host preprocessing with the Laplace filter on the GPU (as CUDACorrelator)."""
+
+    @staticmethod
+    def _laplace_filter(array):
+        return _lib.laplace_wrap(array)
+
+
+@dataclass
+class MapJob:
+    target: np.ndarray
+    template: np.ndarray
+    mask: np.ndarray
+    rotations: np.ndarray
+    laplace: bool = False
+    rot_offset: int = 0
+    flags: int = 0
+    pairs: int = 0                  # rotation pairs per batch (0: autotune)
+    lcc: np.ndarray = field(default=None, repr=False)
+    rot: np.ndarray = field(default=None, repr=False)
+
+
+def scan_queue(jobs, device=0, autotune_trial=256, streams=None):
+    """Scan every job; fills ``job.lcc`` / ``job.rot`` and returns the jobs.
+
+    ``streams``: torch CUDA streams or raw ``cudaStream_t`` handles, one per
+    job (default: a new torch stream per job).
+    """
+    import torch
+    torch.cuda.set_device(device)
+    if streams is None:
+        streams = [torch.cuda.Stream(device=device) for _ in jobs]
+    handles = [s.cuda_stream if hasattr(s, "cuda_stream") else int(s) for s in streams]
+    contexts = []
+    for job, h in zip(jobs, handles):
+        base = _Prep(job.target, laplace=job.laplace)
+        base.template = job.template
+        base.mask = job.mask
+        ctx = _lib.Context(base._target.shape, device)
+        ctx.set_stream(h)
+        ftarget = base._laplace_filter(base._target) if job.laplace else base._target
+        ctx.set_target(ftarget, base._lcc_mask)
+        ctx.set_template_mask(base._template, base._mask, float(base._norm_factor), base._rmax)
+        nrot = ctx.set_rotations(job.rotations)
+        if job.pairs:
+            ctx.set_tuning(pairs=job.pairs)
+        elif autotune_trial:
+            ctx.autotune(min(autotune_trial, nrot))
+        contexts.append((ctx, nrot))
+    # queue every scan before waiting for any
+    for job, (ctx, nrot) in zip(jobs, contexts):
+        ctx.scan_resident(0, nrot, job.rot_offset, job.flags)
+    for job, (ctx, _) in zip(jobs, contexts):
+        job.lcc, job.rot = ctx.get_results()
+    for ctx, _ in contexts:
+        ctx.close()
+    return jobs
+
+
+# The uneven-map workload: 16 seeded maps of 48^3-160^3.
+QUEUE_SIZES = (48, 64, 96, 128, 160)
+
+
+def make_queue(nmaps=16, seed=0):
+    """Seeded maps of uneven size (1.2-2.5 A/voxel, 800-6000 atoms, 5-9 A, SNR 2-6)."""
+    from . import synth
+    rng = np.random.default_rng(seed)
+    cases = []
+    for i in range(nmaps):
+        n = int(QUEUE_SIZES[i % len(QUEUE_SIZES)])
+        vs = float(rng.uniform(1.2, 2.5))
+        natoms = int(rng.integers(800, 6001))
+        res = float(rng.uniform(5.0, 9.0))
+        snr = float(rng.uniform(2.0, 6.0))
+        # keep the chain inside the box
+        natoms = min(natoms, int(1500 * (n * vs / 2.0 / 30.0) ** 3))
+        cases.append(synth.make_case((n, n, n), vs, max(natoms, 200), 1, res, snr, seed * 100 + i))
+    return cases

@@ -280,3 +280,18 @@ def test_split_plane_path_vs_oracle(lib):
     out = lib.Context(a.shape).fft3d(a)
     ref = np.fft.fftn(a.astype(np.float64))
     assert np.max(np.abs(out - ref)) / np.max(np.abs(ref)) < 2e-6
+
+
+def test_map_queue_equals_single_scans():
+    from powerfit_gb300 import synth
+    from powerfit_gb300.queue import MapJob, scan_queue
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    rot = quat_to_rotmat(super_fibonacci(21))
+    jobs = []
+    for i, (n, lap) in enumerate(((48, False), (64, True), (40, False))):
+        c = synth.make_case((n, n, n), 2.0, 500, 2, 8.0, 5.0, 30 + i)
+        jobs.append(MapJob(c.target.astype(np.float64), c.template, c.mask, rot, laplace=lap, pairs=4))
+    scan_queue(jobs)
+    for job in jobs:
+        ref = correlator(job.target, job.template, job.mask, rot, job.laplace)
+        assert np.array_equal(job.lcc, ref.lcc) and np.array_equal(job.rot, ref.rot)
