@@ -67,6 +67,18 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass1_ct(const Pass1Params p, 
   const RotFixed Rb = p.rots[has_b ? rb : 0];
   const double* rda = p.rotd + 9 * (has_a ? ra : 0);
   const double* rdb = p.rotd + 9 * (has_b ? rb : 0);
+  // row part of q = R^T p for both rotations (cz and cy terms), one row per thread
+  __shared__ long long s_q[32][2][3];
+  if (threadIdx.x < nr) {
+    const int4 e = s_row[threadIdx.x];
+    const long long cz = signed_coord(e.x, g.nz), cy = signed_coord(e.y, g.ny);
+    s_q[threadIdx.x][0][0] = Ra.r[6] * cz + Ra.r[3] * cy;
+    s_q[threadIdx.x][0][1] = Ra.r[7] * cz + Ra.r[4] * cy;
+    s_q[threadIdx.x][0][2] = Ra.r[8] * cz + Ra.r[5] * cy;
+    s_q[threadIdx.x][1][0] = Rb.r[6] * cz + Rb.r[3] * cy;
+    s_q[threadIdx.x][1][1] = Rb.r[7] * cz + Rb.r[4] * cy;
+    s_q[threadIdx.x][1][2] = Rb.r[8] * cz + Rb.r[5] * cy;
+  }
   __syncthreads();
 
   // gather the points inside the sphere, spread evenly over the threads
@@ -82,8 +94,8 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass1_ct(const Pass1Params p, 
     else { cx = i - (e.z - 1) / 2; x = cx < 0 ? cx + X : cx; }
     const int cz = signed_coord(e.x, g.nz), cy = signed_coord(e.y, g.ny);
     float ta = 0.f, ma = 0.f, tb = 0.f, mb = 0.f;
-    if (has_a) gather_point(g, p.src, Ra, rda, cz, cy, cx, ta, ma);
-    if (has_b) gather_point(g, p.src, Rb, rdb, cz, cy, cx, tb, mb);
+    if (has_a) gather_point_q(g, p.src, Ra, rda, s_q[c][0], cz, cy, cx, ta, ma);
+    if (has_b) gather_point_q(g, p.src, Rb, rdb, s_q[c][1], cz, cy, cx, tb, mb);
     fld[(0 * p.ty + c) * rs + x] = make_float2(ta, -ma);
     fld[(1 * p.ty + c) * rs + x] = make_float2(tb, -mb);
     fld[(2 * p.ty + c) * rs + x] = make_float2(ma * ma, -(mb * mb));
@@ -168,25 +180,47 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-// Shared-memory bytes of pass 3 for `nbuf` tile buffers.
+// Shared-memory bytes of pass 3 for `nbuf` tile buffers ([3][X][ty] complex).
 __host__ __device__ inline size_t pass3_smem(int X, int ty, int nbuf) {
-  return ((size_t)X + (size_t)nbuf * 3 * ty * (X + kPad)) * sizeof(float2);
+  return ((size_t)X + (size_t)nbuf * 3 * ty * X) * sizeof(float2);
 }
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+// The pass-3 tile keeps the global order: fld[f][kx][r] (r = row of the tile,
+// fastest), so a run of `ty` rows of one (f, kx) is one contiguous copy.
+// Lines of the x transform are (f, r): element kx of line f*ty + r sits at
+// (f*X + kx)*ty + r, consecutive lines are consecutive words.
+struct TileLines {
+  float2* base;
+  int sh, ty, xty;      // log2(ty), ty, X*ty
+  __device__ __forceinline__ int off(int line) const { return (line >> sh) * xty + (line & (ty - 1)); }
+  __device__ __forceinline__ float2 load(int line, int idx) const { return base[off(line) + idx * ty]; }
+  __device__ __forceinline__ void store(int line, int idx, float2 v) const { base[off(line) + idx * ty] = v; }
+};
 
 template <int X>
 __device__ __forceinline__ void pass3_prefetch(const float2* __restrict__ base, float2* fld, int ty, int y0, int ny,
                                                int nz, int z) {
-  // buf[f][kx][z][y0 + r] -> fld[(f*ty + r)*rs + kx]; consecutive threads take consecutive rows (y)
-  constexpr int rs = X + kPad;
-  const int n = 3 * ty * X;
-  const int sh = __ffs(ty) - 1;         // ty is a power of two on this path
-  for (int v = threadIdx.x; v < n; v += kThreadsLine) {
-    const int r = v & (ty - 1);
-    const int fk = v >> sh;             // f * X + kx
-    const int f = fk / X, kx = fk - f * X;
-    float2* dst = fld + (f * ty + r) * rs + kx;
-    if (y0 + r < ny) cp_async8(dst, base + (((long long)f * X + kx) * nz + z) * ny + (y0 + r));
-    else *dst = make_float2(0.f, 0.f);
+  // buf[f][kx][z][y0 .. y0+ty) -> fld[(f*X + kx)*ty .. +ty): 16-byte copies (two rows each)
+  const int halfty = ty >> 1;
+  const int n = 3 * X * halfty;
+  const int sh = __ffs(halfty) - 1;
+  const long long zrow = (long long)z * ny + y0;
+  if (y0 + ty <= ny) {
+    for (int v = threadIdx.x; v < n; v += kThreadsLine) {
+      const int fk = v >> sh, part = v & (halfty - 1);
+      cp_async16(fld + fk * ty + 2 * part, base + (long long)fk * nz * ny + zrow + 2 * part);
+    }
+  } else {   // last tile of an edge not divisible by ty
+    for (int v = threadIdx.x; v < 3 * X * ty; v += kThreadsLine) {
+      const int fk = v / ty, r = v - fk * ty;
+      if (y0 + r < ny) cp_async8(fld + fk * ty + r, base + (long long)fk * nz * ny + zrow + r);
+      else fld[fk * ty + r] = make_float2(0.f, 0.f);
+    }
   }
 }
 
@@ -194,22 +228,24 @@ template <int X>
 __global__ void __launch_bounds__(kThreadsLine, 2) k_pass3_ct(const Pass3Params p) {
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
-  constexpr int rs = X + kPad;
   float2* tw = sm;
   float2* fbuf0 = sm + X;
-  const int fbuf_stride = 3 * p.ty * rs;
+  const int ty = p.ty;                      // a power of two >= 2 on this path
+  const int sh = __ffs(ty) - 1;
+  const int fbuf_stride = 3 * ty * X;
 
   const int z = blockIdx.x;
-  const int y0 = blockIdx.y * p.ty;
-  const int nvox = p.ty * X;
+  const int y0 = blockIdx.y * ty;
+  const int nvox = ty * X;
   const long long zoff = (long long)z * g.ny * X;
   const long long fstride = (long long)X * g.nz * g.ny;
 
   // start the first tile's copies before anything else
-  pass3_prefetch<X>(p.buf, fbuf0, p.ty, y0, g.ny, g.nz, z);
+  pass3_prefetch<X>(p.buf, fbuf0, ty, y0, g.ny, g.nz, z);
   cp_async_commit();
   for (int i = threadIdx.x; i < X; i += kThreadsLine) tw[i] = p.twx[i];
 
+  // voxel v of the tile: row r = v & (ty-1), column x = v >> log2(ty)
   float best[kMaxVoxPerThread];
   int brot[kMaxVoxPerThread];
   unsigned int inmask = 0;
@@ -219,7 +255,7 @@ __global__ void __launch_bounds__(kThreadsLine, 2) k_pass3_ct(const Pass3Params 
     best[k] = 0.f;
     brot[k] = 0;
     if (v < nvox) {
-      const int r = v / X, x = v - r * X;
+      const int r = v & (ty - 1), x = v >> sh;
       const int y = y0 + r;
       if (y < g.ny) {
         const long long gi = zoff + (long long)y * X + x;
@@ -233,7 +269,7 @@ __global__ void __launch_bounds__(kThreadsLine, 2) k_pass3_ct(const Pass3Params 
   for (int pair = 0; pair < p.npairs; ++pair) {
     float2* fld = fbuf0 + (pair & 1) * fbuf_stride;
     if (pair + 1 < p.npairs) {
-      pass3_prefetch<X>(p.buf + (long long)(pair + 1) * 3 * fstride, fbuf0 + ((pair + 1) & 1) * fbuf_stride, p.ty, y0,
+      pass3_prefetch<X>(p.buf + (long long)(pair + 1) * 3 * fstride, fbuf0 + ((pair + 1) & 1) * fbuf_stride, ty, y0,
                         g.ny, g.nz, z);
       cp_async_commit();
       cp_async_wait_group<1>();
@@ -241,18 +277,19 @@ __global__ void __launch_bounds__(kThreadsLine, 2) k_pass3_ct(const Pass3Params 
       cp_async_wait_group<0>();
     }
     __syncthreads();
-    SmemLines lines{fld, rs, 1};
-    ct_lines<X, true, kThreadsLine, kEmax>(3 * p.ty, tw, lines, lines, lines, true, true);
+    TileLines lines{fld, sh, ty, X * ty};
+    ct_lines<X, true, kThreadsLine, kEmax>(3 * ty, tw, lines, lines, lines, true, true);
     const long long ra = p.first_rot + 2LL * pair;
     const bool has_b = ra + 1 < p.nrot;
 #pragma unroll
     for (int k = 0; k < kMaxVoxPerThread; ++k) {
       if (inmask & (1u << k)) {
         const int v = threadIdx.x + k * kThreadsLine;
-        const int r = v / X, x = v - r * X;
-        const float2 f0 = fld[(0 * p.ty + r) * rs + x];
-        const float2 f1 = fld[(1 * p.ty + r) * rs + x];
-        const float2 f2 = fld[(2 * p.ty + r) * rs + x];
+        const int r = v & (ty - 1), x = v >> sh;
+        const int o = x * ty + r;
+        const float2 f0 = fld[o];
+        const float2 f1 = fld[X * ty + o];
+        const float2 f2 = fld[2 * X * ty + o];
         float la, lb;
         if (p.fp64) {
           la = lcc_value64(f0.x, f0.y, f2.x, p.norm_factor);
@@ -271,7 +308,7 @@ __global__ void __launch_bounds__(kThreadsLine, 2) k_pass3_ct(const Pass3Params 
   for (int k = 0; k < kMaxVoxPerThread; ++k) {
     const int v = threadIdx.x + k * kThreadsLine;
     if (v < nvox) {
-      const int r = v / X, x = v - r * X;
+      const int r = v & (ty - 1), x = v >> sh;
       const int y = y0 + r;
       if (y < g.ny) {
         const long long gi = zoff + (long long)y * X + x;
