@@ -102,6 +102,7 @@ struct pf_ctx {
   AxisPlan px{}, py{}, pz{};
   float2 *twx = nullptr, *twy = nullptr, *twz = nullptr;
   float *tmpl = nullptr, *mask = nullptr;
+  float2* tmpl_pairs = nullptr;      // fast pass 1: template as x-neighbour pairs
   unsigned char* lcc_mask = nullptr;
   float2* spec = nullptr;          // [2][kx][kz][ky]
   float* lcc = nullptr;
@@ -181,9 +182,11 @@ void choose_tiles(pf_ctx* c) {
   c->ty1 = ty;
   // pass 3: every voxel of a tile owned by one thread slot; enough tiles to
   // fill the machine (>= 4 per SM on 152 SMs)
-  int ty3 = 16;   // a power of two (the fast pass 3 splits tile indices with shifts)
-  while (ty3 > 1 && (long long)ty3 * X > (long long)kMaxVoxPerThread * kThreadsLine) ty3 /= 2;
-  while (ty3 > 2 && (long long)c->nz * ((c->ny + ty3 - 1) / ty3) < 4 * 152) ty3 /= 2;
+  // a power of two (>= 2 on the fast path, whose pass 3 copies two rows per 16 bytes)
+  const int ty3_min = c->fast ? 2 : 1;
+  int ty3 = 16;
+  while (ty3 > ty3_min && (long long)ty3 * X > (long long)kMaxVoxPerThread * kThreadsLine) ty3 /= 2;
+  while (ty3 > ty3_min && (long long)c->nz * ((c->ny + ty3 - 1) / ty3) < 4 * 152) ty3 /= 2;
   c->ty3 = ty3;
   // pairs per batch: intermediate spectra of one batch <= 64 MiB (L2-sized), at least 1, at most 16
   const long long per_pair = 3LL * c->N * (long long)sizeof(float2);
@@ -490,7 +493,7 @@ int pf_destroy(pf_ctx* c) {
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   c->own_stream = nullptr;
   void* ptrs[] = {c->twx, c->twy, c->twz, c->tmpl, c->mask, c->lcc_mask, c->spec, c->lcc, c->rot, c->buf, c->rots, c->rotd,
-                  c->rows_reach, c->rows_full};
+                  c->rows_reach, c->rows_full, c->tmpl_pairs};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete c;
@@ -559,7 +562,12 @@ int pf_set_template_mask(pf_ctx* c, const double* tmpl, const double* mask, doub
   if (c->fast) {
     int rc2 = build_rows(c, std::min(rmax, reff), &c->rows_reach, &c->nrows_reach);
     if (!rc2) rc2 = build_rows(c, rmax, &c->rows_full, &c->nrows_full);
+    if (!rc2 && !c->tmpl_pairs) rc2 = alloc(c, (void**)&c->tmpl_pairs, c->N * sizeof(float2));
     if (rc2) return rc2;
+    k_make_pairs<<<(unsigned)std::min<long long>((c->N + 255) / 256, 8192), 256, 0, c->stream>>>(c->tmpl, c->tmpl_pairs,
+                                                                                             c->nx, c->N);
+    PF_CUDA(c, cudaGetLastError());
+    PF_CUDA(c, cudaStreamSynchronize(c->stream));
   }
   c->have_template = true;
   return PF_OK;
@@ -635,7 +643,7 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
   for (int64_t r0 = first; r0 < end; r0 += 2LL * P) {
     const int npairs = (int)std::min<int64_t>(P, (end - r0 + 1) / 2);
     const bool full = (flags & PF_FLAG_NO_PRUNE) != 0;
-    Pass1Params p1{g, c->px, GatherSrc{c->tmpl, c->mask}, c->twx, c->rots, c->rotd, r0, end, c->buf, ty1,
+    Pass1Params p1{g, c->px, GatherSrc{c->tmpl, c->mask, c->tmpl_pairs}, c->twx, c->rots, c->rotd, r0, end, c->buf, ty1,
                    full ? c->rows_full : c->rows_reach, full ? c->nrows_full : c->nrows_reach};
     rc = timed_launch(c, 0, [&] {
       if (fast) {
@@ -717,7 +725,8 @@ int pf_set_tuning(pf_ctx* c, int pairs, int rows1, int rows3) {
   if (rows1 && (!ok_rows(rows1) || rows1 > 32)) return fail(c, PF_E_ARG, "rows_pass1 %d too large for nx %d", rows1, c->nx);
   if (rows3 && (!ok_rows(rows3) || (long long)rows3 * c->nx > (long long)kMaxVoxPerThread * kThreadsLine))
     return fail(c, PF_E_ARG, "rows_pass3 %d too large for nx %d", rows3, c->nx);
-  if (rows3 && (rows3 & (rows3 - 1))) return fail(c, PF_E_ARG, "rows_pass3 must be a power of two");
+  if (rows3 && ((rows3 & (rows3 - 1)) || (c->fast && rows3 < 2)))
+    return fail(c, PF_E_ARG, "rows_pass3 must be a power of two (>= 2 for this grid)");
   if (pairs) {
     DeviceGuard guard(c->device);
     cudaStreamSynchronize(c->stream);
