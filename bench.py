@@ -201,6 +201,26 @@ def bytes_per_rotation(n, B):
     return 8 * N + 8 * H * (2 * 3 + 6) + (16 * H + 17 * N) / B
 
 
+def dram_traffic(kernel, n, pairs_per_launch):
+    """DRAM bytes per launch of ``kernel`` at grid n^3 from the committed ncu
+    summary (read + write of one captured launch), scaled from the captured
+    launch's rotation pairs to this run's; (None, reason) without an entry."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    try:
+        for ln in open(path):
+            parts = ln.split()
+            if len(parts) >= 5 and not ln.startswith("#") and parts[0] == kernel and int(parts[1]) == n:
+                cap_pairs, rd, wr = int(parts[2]), float(parts[3]), float(parts[4])
+                scale = pairs_per_launch / cap_pairs
+                note = "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/dram_traffic.txt"
+                if abs(scale - 1.0) > 1e-9:
+                    note += " (captured at %d pairs per launch, scaled to %g)" % (cap_pairs, pairs_per_launch)
+                return (rd + wr) * scale, note
+    except (OSError, ValueError):
+        pass
+    return None, "no ncu capture for %s at %d^3" % (kernel, n)
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     cores = os.cpu_count() or 1
@@ -327,6 +347,7 @@ def run_ours(args, rank, world, local_rank):
 
     # roofline of the dominant kernel: algorithmic bytes per launch / average launch time
     names = ["pass1_rotate_fwdx", "pass2_yz_product", "pass3_invx_lcc"]
+    kernels = ["k_pass1_ct", "k_pass2_ct", "k_pass3_ct"]
     dom = int(np.argmax(kms))
     launches = int(klaunch.sum())
     nz, ny, nx = shape
@@ -335,15 +356,22 @@ def run_ours(args, rank, world, local_rank):
     cy = np.where(2 * np.arange(ny) <= ny, np.arange(ny), np.arange(ny) - ny)
     disk = int(np.sum(cz[:, None] ** 2 + cy[None, :] ** 2 <= re * re))   # (z, y) rows the rotation reaches
     pairs_per_launch = done / 2.0 / max(int(klaunch[dom]), 1)
-    per_pair = {
-        # template + mask read once (L2-resident), 3 spectra rows written for the disk rows
-        0: 8 * N / pairs_per_launch + 3 * 8 * disk * nx,
-        # per (field, kx) plane: disk entries read, full plane written, target spectrum plane read
-        1: 3 * nx * 8 * (disk + 2 * nz * ny),
-        # 3 spectra read; lcc + rot read and written and the lcc mask read once per launch
+    B = 2.0 * pairs_per_launch                                         # rotations per launch
+    H = nz * ny * (nx // 2 + 1)
+    F = 3
+    # the streaming pipeline model 8N + 8H(2F+6) + (16H+17N)/B, split by the pass that moves the bytes
+    per_rot = {
+        0: 8 * N + 8 * H * F,                     # template + mask read, F forward spectra written
+        1: 8 * H * F + 8 * H * 3 + 16 * H / B,    # F spectra read, 3 product spectra written, target spectra once
+        2: 8 * H * 3 + 17 * N / B,                # 3 product spectra read; lcc mask, lcc, rot once per launch
+    }
+    # what the pruned kernels move (complex64 full planes of a rotation pair, rows outside the reach disk skipped)
+    pruned_per_pair = {
+        0: 8 * N / pairs_per_launch + 3 * 8 * disk * nx,      # template + mask once, disk rows of 3 spectra written
+        1: 3 * nx * 8 * (disk + nz * ny) + 16 * N / pairs_per_launch,
         2: 3 * 8 * N + (17 * N) / pairs_per_launch,
     }
-    alg_bytes = per_pair[dom] * pairs_per_launch
+    alg_bytes = per_rot[dom] * B
     avg_s = kms[dom] / 1e3 / max(int(klaunch[dom]), 1)
     peaks = {}
     try:
@@ -352,8 +380,9 @@ def run_ours(args, rank, world, local_rank):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = alg_bytes / avg_s / 1e9
+    traffic, traffic_src = dram_traffic(kernels[dom], n, pairs_per_launch)
     pipe_bytes = bytes_per_rotation(n, 2 * pairs)
-    pruned_bytes = sum(per_pair.values()) / 2.0
+    pruned_bytes = sum(pruned_per_pair.values()) / 2.0
     line = {
         "metric": metric_for(shape), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
@@ -377,8 +406,8 @@ def run_ours(args, rank, world, local_rank):
         "kernel_share": {names[i]: float(kms[i] / kms.sum()) for i in range(3)},
         "profiled_pass_s": prof_s,
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "bytes_per_launch": alg_bytes,
+                     "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+                     "bytes_per_launch": alg_bytes, "pruned_bytes_per_launch": pruned_per_pair[dom] * pairs_per_launch,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s"},
         "pipeline_roofline": {"model": "streaming 3-pass, unpruned: 8N + 8H(2F+6) + (16H+17N)/B",
                               "bytes_per_rotation": pipe_bytes, "achieved_gbs": pipe_bytes * value / world / 1e9,
@@ -475,7 +504,7 @@ def run_precision(args):
     line = {"metric": "precision vs float64 oracle", "config": {"workload": args.config, "grid": list(target.shape),
             "rotations": int(sub.shape[0]), "laplace": cfg["laplace"], "core_weighted": cfg["core_weighted"]},
             "variants": res, "oracle_s": oracle_s, "oracle_cores": cores,
-            "note": "a split-bf16x3 tensor-core DFT variant is not built (see DESIGN.md)"}
+            "note": "a split-bf16x3 tensor-core DFT variant is not built: the path is HBM- and latency-bound"}
     print(json.dumps(line), flush=True)
     return 0
 
