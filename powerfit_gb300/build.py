@@ -40,8 +40,21 @@ def nvcc():
     raise RuntimeError("nvcc not found")
 
 
+STAMP = os.path.join(OBJ_DIR, "flags.txt")
+
+
+def extra_flags():
+    """Build-variant knob (e.g. ``-DPF_PACKED_F32X2=0``)."""
+    return os.environ.get("POWERFIT_NVCC_FLAGS", "").split()
+
+
 def up_to_date():
     if not os.path.exists(LIB):
+        return False
+    try:
+        if open(STAMP).read() != " ".join(extra_flags()):
+            return False          # built with other variant flags
+    except OSError:
         return False
     t = os.path.getmtime(LIB)
     return all(os.path.getmtime(d) <= t for d in deps())
@@ -49,8 +62,7 @@ def up_to_date():
 
 def _compile(src, verbose):
     obj = os.path.join(OBJ_DIR, os.path.basename(src)[:-3] + ".o")
-    extra = os.environ.get("POWERFIT_NVCC_FLAGS", "").split()   # build-variant knob (e.g. -DPF_PACKED_F32X2=0)
-    cmd = [nvcc()] + ARCH + FLAGS + extra + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + ARCH + FLAGS + extra_flags() + ["-c", src, "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     res = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
@@ -76,6 +88,8 @@ def build(force=False, verbose=False, jobs=None):
     if res.returncode != 0:
         raise RuntimeError("link failed:\n" + res.stdout)
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(" ".join(extra_flags()))
     return LIB
 
 

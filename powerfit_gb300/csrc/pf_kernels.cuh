@@ -32,6 +32,15 @@ namespace pf {
 constexpr int kEmax = 16;          // complex values a thread holds per stage chunk
 constexpr int kThreadsLine = 256;  // pass 1 / pass 3 / target x transform
 constexpr int kThreadsPlane = 512; // pass 2 / target (y, z) transform
+// resident pass-1 blocks per SM that the register allocation must allow (0: compiler's choice)
+#ifndef PF_PASS1_MIN_BLOCKS
+#define PF_PASS1_MIN_BLOCKS 4
+#endif
+#if PF_PASS1_MIN_BLOCKS > 0
+#define PF_PASS1_BOUNDS __launch_bounds__(kThreadsLine, PF_PASS1_MIN_BLOCKS)
+#else
+#define PF_PASS1_BOUNDS __launch_bounds__(kThreadsLine)
+#endif
 constexpr int kPad = 1;            // shared-memory row padding (complex) for conflict-free access
 
 // 32.32 fixed-point rotation matrix (row-major R, element r_i = round(R_i * 2^32))

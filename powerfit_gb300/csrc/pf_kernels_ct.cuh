@@ -37,7 +37,7 @@ struct RowListStore {  // line = f*ty + c (row c of the chunk); idx = kx
 // host from the template's support): every block transforms `ty` such rows,
 // none is empty and none is outside the reach.
 template <int X>
-__global__ void __launch_bounds__(kThreadsLine) k_pass1_ct(const Pass1Params p, const int re2) {
+__global__ void PF_PASS1_BOUNDS k_pass1_ct(const Pass1Params p, const int re2) {
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
   constexpr int rs = X + kPad;
@@ -121,8 +121,20 @@ struct SpectrumOperand {  // target spectrum plane [kz][ky] of this kx
   __device__ __forceinline__ float2 fetch(int ky, int kz) const { return __ldg(spec + (long long)kz * ny + ky); }
 };
 
+// Block shape of the plane pass: a plane of 128 x 128 or more fills one block
+// per SM (shared memory), which then runs 1024 threads; smaller planes run two
+// 512-thread blocks per SM.  Both leave 64 registers a thread.
 template <int Y, int Z>
-__global__ void __launch_bounds__(kThreadsPlane, 1) k_pass2_ct(const Pass2Params p, const int re2) {
+struct PlaneLaunch {
+  static constexpr bool kBig = Y * Z >= 128 * 128;
+  static constexpr int kThreads = kBig ? 1024 : 512;
+  static constexpr int kMinBlocks = kBig ? 1 : 2;
+};
+
+template <int Y, int Z>
+__global__ void __launch_bounds__(PlaneLaunch<Y, Z>::kThreads, PlaneLaunch<Y, Z>::kMinBlocks)
+    k_pass2_ct(const Pass2Params p, const int re2) {
+  constexpr int kThreadsPlaneCt = PlaneLaunch<Y, Z>::kThreads;
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
   constexpr int rs = Y + kPad;
@@ -138,35 +150,35 @@ __global__ void __launch_bounds__(kThreadsPlane, 1) k_pass2_ct(const Pass2Params
 
   // copy-in: asynchronous 8-byte copies of the rows the rotation can reach,
   // zeros elsewhere (every thread keeps many copies in flight)
-  for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlane) {
+  for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlaneCt) {
     const int z = v / Y, y = v - z * Y;
     const bool valid = p.mode != 0 ||
                        ((z <= lo_end || z >= hi_start) && row_in_disk(g, signed_coord(z, Z), signed_coord(y, Y), re2));
     if (valid) cp_async8(pl + z * rs + y, gplane + (long long)z * Y + y);
     else pl[z * rs + y] = make_float2(0.f, 0.f);
   }
-  for (int i = threadIdx.x; i < Y; i += kThreadsPlane) twy[i] = p.twy[i];
-  for (int i = threadIdx.x; i < Z; i += kThreadsPlane) twz[i] = p.twz[i];
+  for (int i = threadIdx.x; i < Y; i += kThreadsPlaneCt) twy[i] = p.twy[i];
+  for (int i = threadIdx.x; i < Z; i += kThreadsPlaneCt) twz[i] = p.twz[i];
   cp_async_wait_all();
   __syncthreads();
 
   RowMapLines rows{pl, rs, g.zlo, Z - nvz};
-  ct_lines<Y, false, kThreadsPlane, kEmax>(nvz, twy, rows, rows, rows, true, true);
+  ct_lines<Y, false, kThreadsPlaneCt, kEmax>(nvz, twy, rows, rows, rows, true, true);
   SmemLines cols{pl, 1, rs};
   if (p.mode == 0) {
     const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + (long long)kx * plane;
-    ct_fwd_mul_inv<Z, kThreadsPlane, kEmax>(Y, twz, cols, SpectrumOperand{spec, Y});
+    ct_fwd_mul_inv<Z, kThreadsPlaneCt, kEmax>(Y, twz, cols, SpectrumOperand{spec, Y});
     SmemLines allrows{pl, rs, 1};
-    ct_lines<Y, true, kThreadsPlane, kEmax>(Z, twy, allrows, allrows, allrows, true, true);
+    ct_lines<Y, true, kThreadsPlaneCt, kEmax>(Z, twy, allrows, allrows, allrows, true, true);
 #pragma unroll 4
-    for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlane) {
+    for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlaneCt) {
       const int z = v / Y, y = v - z * Y;
       gplane[(long long)z * Y + y] = pl[z * rs + y];
     }
   } else {
-    ct_lines<Z, false, kThreadsPlane, kEmax>(Y, twz, cols, cols, cols, true, true);
+    ct_lines<Z, false, kThreadsPlaneCt, kEmax>(Y, twz, cols, cols, cols, true, true);
     float2* o = p.out + ((long long)f * g.nx + kx) * plane;
-    for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlane) {
+    for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlaneCt) {
       const int z = v / Y, y = v - z * Y;
       o[(long long)z * Y + y] = cscale(pl[z * rs + y], p.scale);
     }
@@ -333,7 +345,7 @@ struct FastSize {
     k_pass1_ct<N><<<grid, kThreadsLine, smem, s>>>(p, re2);
   }
   static void pass2(const Pass2Params& p, int re2, dim3 grid, size_t smem, cudaStream_t s) {
-    k_pass2_ct<N, N><<<grid, kThreadsPlane, smem, s>>>(p, re2);
+    k_pass2_ct<N, N><<<grid, PlaneLaunch<N, N>::kThreads, smem, s>>>(p, re2);
   }
   static void pass3(const Pass3Params& p, dim3 grid, size_t smem, cudaStream_t s) {
     k_pass3_ct<N><<<grid, kThreadsLine, smem, s>>>(p);
