@@ -89,7 +89,8 @@ RotFixed to_fixed(const double* r) {
 }
 
 size_t line_smem(int X, int nf, int ty) { return ((size_t)X + (size_t)nf * ty * (X + kPad)) * sizeof(float2); }
-size_t plane_smem(int Y, int Z) { return ((size_t)Y + Z + (size_t)Z * (Y + kPad)) * sizeof(float2); }
+// twiddles (y, z), the plane [Z][Y + kPad], the last inverse-y stage's twiddle table (Y)
+size_t plane_smem(int Y, int Z) { return ((size_t)Y + Z + (size_t)Z * (Y + kPad) + Y) * sizeof(float2); }
 
 }  // namespace
 

@@ -167,16 +167,111 @@ __device__ __forceinline__ void ct_lines(int nlines, const float2* __restrict__ 
 }
 
 
-// Forward stages 0 .. nst-2 in place (all but the last).
-template <int L, int NT, int EMAX, int S, class Mid>
-__device__ __forceinline__ void ct_fwd_head(int nlines, const float2* __restrict__ tw, const Mid& mid) {
+// Forward stages 0 .. nst-2 in place (all but the last); stage 0 reads `src`
+// (which aliases `mid` when `src_alias`).
+template <int L, int NT, int EMAX, int S, class Src, class Mid>
+__device__ __forceinline__ void ct_fwd_head(int nlines, const float2* __restrict__ tw, const Src& src,
+                                            const Mid& mid, bool src_alias) {
   constexpr CtPlan P = ct_plan(L);
   if constexpr (S < P.nst - 1) {
     constexpr int R = P.r[S];
     constexpr int NS = ct_stage_ns(L, S);
-    ct_stage<R, false, L, NS, NT, EMAX>(nlines, tw, mid, mid, true);
+    if constexpr (S == 0) ct_stage<R, false, L, NS, NT, EMAX>(nlines, tw, src, mid, src_alias);
+    else ct_stage<R, false, L, NS, NT, EMAX>(nlines, tw, mid, mid, true);
     __syncthreads();
-    ct_fwd_head<L, NT, EMAX, S + 1>(nlines, tw, mid);
+    ct_fwd_head<L, NT, EMAX, S + 1>(nlines, tw, src, mid, src_alias);
+  }
+}
+
+// First stage (Ns = 1, no twiddles) of a length-L transform over at most LMAX
+// lines in a single chunk: every item is loaded from `src` and transformed
+// before `bar()` runs, and stored to `dst` after it.  With a cluster-wide
+// barrier this lets a block read other blocks' shared memory and then
+// overwrite its own, which those blocks were reading.
+template <int R, bool INV, int L, int NT, int LMAX, class Src, class Dst, class Bar>
+__device__ __forceinline__ void ct_first_stage_gather(int nlines, const Src& src, const Dst& dst, const Bar& bar) {
+  constexpr int NB = L / R;
+  constexpr int K = (LMAX * NB + NT - 1) / NT;       // items (line, butterfly) per thread
+  float2 v[K][R];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int it = threadIdx.x + k * NT;
+    const int line = it % LMAX;                      // consecutive threads take consecutive lines
+    const int j = it / LMAX;
+    if (j < NB && line < nlines) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[k][r] = src.load(line, j + r * NB);
+      DFT<R, INV>::run(v[k]);
+    }
+  }
+  bar();
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int it = threadIdx.x + k * NT;
+    const int line = it % LMAX;
+    const int j = it / LMAX;
+    if (j < NB && line < nlines) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) dst.store(line, j * R + r, v[k][r]);
+    }
+  }
+}
+
+// Stages 0 .. nst-2 of a length-L transform, in place in `mid`, each followed
+// by a barrier.
+template <int L, bool INV, int NT, int EMAX, int S, class Mid>
+__device__ __forceinline__ void ct_head_inplace(int nlines, const float2* __restrict__ tw, const Mid& mid) {
+  constexpr CtPlan P = ct_plan(L);
+  if constexpr (S < P.nst - 1) {
+    constexpr int R = P.r[S];
+    constexpr int NS = ct_stage_ns(L, S);
+    ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, mid, mid, true);
+    __syncthreads();
+    ct_head_inplace<L, INV, NT, EMAX, S + 1>(nlines, tw, mid);
+  }
+}
+
+// Twiddles of the last stage as an [r][j] table: tl[r * NB + j] = tw[r * j],
+// NB = L / R_last (the last stage has Ns = NB, so butterfly j of it multiplies
+// input r by tw[r * j]).
+template <int L, int NT>
+__device__ __forceinline__ void ct_last_twiddles(const float2* __restrict__ tw, float2* tl) {
+  constexpr CtPlan P = ct_plan(L);
+  constexpr int NB = L / P.r[P.nst - 1];
+  for (int i = threadIdx.x; i < L; i += NT) {
+    const int r = i / NB, j = i - r * NB;
+    tl[i] = tw[r * j];
+  }
+}
+
+// Last stage of a length-L transform with the items mapped butterfly-fastest
+// (consecutive threads take consecutive butterflies j of one line), reading
+// `mid` and writing `out`.  Its stores y[j + r Ns] from consecutive threads
+// cover consecutive elements of a line, so `out` may be global memory, written
+// in whole segments straight from registers.  `tl` is the [r][j] table above.
+template <int L, bool INV, int NT, class Mid, class Out>
+__device__ __forceinline__ void ct_last_stage_out(int nlines, const float2* __restrict__ tl, const Mid& mid,
+                                                  const Out& out) {
+  constexpr CtPlan P = ct_plan(L);
+  constexpr int R = P.r[P.nst - 1];
+  constexpr int NB = L / R;
+  const int total = nlines * NB;
+  for (int it = threadIdx.x; it < total; it += NT) {
+    const int line = it / NB, j = it - line * NB;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = mid.load(line, j + r * NB);
+    if constexpr (P.nst > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        float2 w = tl[r * NB + j];
+        if (INV) w.y = -w.y;
+        v[r] = cmul(v[r], w);
+      }
+    }
+    DFT<R, INV>::run(v);
+#pragma unroll
+    for (int r = 0; r < R; ++r) out.store(line, j + r * NB, v[r]);
   }
 }
 
@@ -215,14 +310,17 @@ __device__ __forceinline__ void ct_rev_from(int nlines, const float2* __restrict
 // ``mul(line, k, v)`` and the inverse's first stage (reversed plan) run on the
 // same registers: radix R_last with Ns = L/R_last stores y[j + r L/R], which
 // is exactly what a first stage (Ns = 1) of radix R_last loads.
-template <int L, int NT, int EMAX, class Mid, class Mul>
+//
+// The forward's first stage reads `src` (by default `mid` itself); `src_alias`
+// says whether it shares memory with `mid`.
+template <int L, int NT, int EMAX, class Mid, class Mul, class Src = Mid>
 __device__ __forceinline__ void ct_fwd_mul_inv(int nlines, const float2* __restrict__ tw, const Mid& mid,
-                                               const Mul& mul) {
+                                               const Mul& mul, const Src& src, bool src_alias) {
   constexpr CtPlan P = ct_plan(L);
   constexpr int RL = P.r[P.nst - 1];
   constexpr int NB = L / RL;
   // forward stages 0 .. nst-2
-  ct_fwd_head<L, NT, EMAX, 0>(nlines, tw, mid);
+  ct_fwd_head<L, NT, EMAX, 0>(nlines, tw, src, mid, src_alias);
   // fused stage
   constexpr int KMAX = (EMAX / RL) > 0 ? (EMAX / RL) : 1;
   constexpr int C0 = (NT * KMAX) / NB;
@@ -240,7 +338,10 @@ __device__ __forceinline__ void ct_fwd_mul_inv(int nlines, const float2* __restr
 #pragma unroll
         for (int r = 0; r < RL; ++r) m[r] = mul.fetch(line, j + r * NB);   // issue the operand loads early
 #pragma unroll
-        for (int r = 0; r < RL; ++r) v[k][r] = mid.load(line, j + r * NB);
+        for (int r = 0; r < RL; ++r) {
+          if constexpr (P.nst == 1) v[k][r] = src.load(line, j + r * NB);   // the only stage is the first
+          else v[k][r] = mid.load(line, j + r * NB);
+        }
         if constexpr (NB > 1) {           // forward last stage twiddles (Ns = NB)
           const int jm = j;               // (j % NB) * (L / (NB * RL)) with L / (NB * RL) == 1
 #pragma unroll

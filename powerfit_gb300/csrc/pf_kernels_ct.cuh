@@ -7,6 +7,7 @@
 // for it without touching memory.
 #pragma once
 #include <algorithm>
+#include <cooperative_groups.h>
 #include "pf_fft_ct.cuh"
 #include "pf_kernels.cuh"
 
@@ -115,6 +116,12 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+struct GlobalRows {  // rows of a plane in global memory: line = z, idx = y
+  float2* __restrict__ base;
+  int ny;
+  __device__ __forceinline__ void store(int line, int idx, float2 v) const { base[(long long)line * ny + idx] = v; }
+};
+
 struct SpectrumOperand {  // target spectrum plane [kz][ky] of this kx
   const float2* __restrict__ spec;
   int ny;
@@ -141,6 +148,7 @@ __global__ void __launch_bounds__(PlaneLaunch<Y, Z>::kThreads, PlaneLaunch<Y, Z>
   float2* twy = sm;
   float2* twz = sm + Y;
   float2* pl = sm + Y + Z;
+  float2* tly = pl + Z * rs;     // last inverse-y stage twiddles, [r][j]
 
   const int kx = blockIdx.x, f = blockIdx.y, pair = blockIdx.z;
   constexpr long long plane = (long long)Z * Y;
@@ -159,6 +167,7 @@ __global__ void __launch_bounds__(PlaneLaunch<Y, Z>::kThreads, PlaneLaunch<Y, Z>
   }
   for (int i = threadIdx.x; i < Y; i += kThreadsPlaneCt) twy[i] = p.twy[i];
   for (int i = threadIdx.x; i < Z; i += kThreadsPlaneCt) twz[i] = p.twz[i];
+  ct_last_twiddles<Y, kThreadsPlaneCt>(p.twy, tly);
   cp_async_wait_all();
   __syncthreads();
 
@@ -167,14 +176,11 @@ __global__ void __launch_bounds__(PlaneLaunch<Y, Z>::kThreads, PlaneLaunch<Y, Z>
   SmemLines cols{pl, 1, rs};
   if (p.mode == 0) {
     const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + (long long)kx * plane;
-    ct_fwd_mul_inv<Z, kThreadsPlaneCt, kEmax>(Y, twz, cols, SpectrumOperand{spec, Y});
+    ct_fwd_mul_inv<Z, kThreadsPlaneCt, kEmax>(Y, twz, cols, SpectrumOperand{spec, Y}, cols, true);
+    // inverse y: all stages but the last in place, the last one straight to the buffer
     SmemLines allrows{pl, rs, 1};
-    ct_lines<Y, true, kThreadsPlaneCt, kEmax>(Z, twy, allrows, allrows, allrows, true, true);
-#pragma unroll 4
-    for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlaneCt) {
-      const int z = v / Y, y = v - z * Y;
-      gplane[(long long)z * Y + y] = pl[z * rs + y];
-    }
+    ct_head_inplace<Y, true, kThreadsPlaneCt, kEmax, 0>(Z, twy, allrows);
+    ct_last_stage_out<Y, true, kThreadsPlaneCt>(Z, tly, allrows, GlobalRows{gplane, Y});
   } else {
     ct_lines<Z, false, kThreadsPlaneCt, kEmax>(Y, twz, cols, cols, cols, true, true);
     float2* o = p.out + ((long long)f * g.nx + kx) * plane;
@@ -184,6 +190,159 @@ __global__ void __launch_bounds__(PlaneLaunch<Y, Z>::kThreads, PlaneLaunch<Y, Z>
     }
   }
 }
+
+// ---------------------------------------------------------------------------
+// Pass 2 (fast, clustered): the plane of one (pair, field, kx) shared by a
+// cluster of CS blocks, each holding 1/CS of it, so that a 128 x 128 plane
+// leaves room for two blocks per SM.
+//
+//   A. block c copies in and y-transforms its share of the valid z rows
+//      (rb = ceil(nvz / CS) rows from valid row c*rb on);
+//   B. it z-transforms its CW = Y/CS columns: the first stage reads the rows
+//      from every block's shared memory (distributed shared memory), the
+//      product and the inverse z run in its own column array;
+//   C. it inverse-y-transforms its ZB = Z/CS z rows: the first stage reads
+//      the columns from every block, and, after a cluster barrier, stores
+//      into its own column array (as rows); then it writes its rows out.
+//
+// Three cluster barriers order the exchange: rows complete before B, columns
+// complete before C, every read of C done before C's stores.  No block reads
+// another's memory after the last one, so a block may exit right after it.
+// ---------------------------------------------------------------------------
+template <int CS>
+struct ClusterPeers {  // the same shared-memory array in each block of the cluster
+  float2* p[CS];
+  __device__ __forceinline__ float2* get(int r) const {
+    float2* q = p[0];
+#pragma unroll
+    for (int k = 1; k < CS; ++k) q = (r == k) ? p[k] : q;
+    return q;
+  }
+};
+
+template <int Y, int CS>
+struct ClusterRowsSrc {  // z transform input: line = own column (ky - ky0), idx = z
+  ClusterPeers<CS> rows;  // valid rows, rb per block, row stride Y + kPad
+  int ky0, zlo, hi_start, shift, rb;
+  __device__ __forceinline__ float2 load(int line, int z) const {
+    if (z > zlo && z < hi_start) return make_float2(0.f, 0.f);   // plane the rotation cannot reach
+    const int i = z <= zlo ? z : z - shift;                        // valid-row index
+    int owner = 0;
+#pragma unroll
+    for (int k = 1; k < CS; ++k) owner += (i >= k * rb) ? 1 : 0;
+    return rows.get(owner)[(i - owner * rb) * (Y + kPad) + ky0 + line];
+  }
+};
+
+template <int Y, int CS>
+struct ClusterColsSrc {  // inverse y input: line = own z row (z - z0), idx = ky
+  static constexpr int CW = Y / CS;
+  ClusterPeers<CS> cols;  // column arrays [z][CW + kPad]
+  int z0;
+  __device__ __forceinline__ float2 load(int line, int ky) const {
+    const int owner = ky / CW;
+    return cols.get(owner)[(z0 + line) * (CW + kPad) + ky - owner * CW];
+  }
+};
+
+struct ClusterBarrier {
+  __device__ __forceinline__ void operator()() const { cooperative_groups::this_cluster().sync(); }
+};
+
+template <int Y, int Z, int CS>
+struct ClusterPlane {
+  static constexpr int kThreads = 512;
+  static constexpr int kCW = Y / CS;   // columns per block
+  static constexpr int kZB = Z / CS;   // z rows per block after the z transform
+  static_assert(Y % CS == 0 && Z % CS == 0, "cluster must divide the plane");
+  // shared memory: twiddles, column array [Z][CW + kPad], row array [rb][Y + kPad]
+  static size_t smem(int nvz) {
+    const int rb = (nvz + CS - 1) / CS;
+    return ((size_t)Y + Z + (size_t)Z * (kCW + kPad) + (size_t)rb * (Y + kPad)) * sizeof(float2);
+  }
+};
+
+template <int Y, int Z, int CS>
+__global__ void __launch_bounds__(ClusterPlane<Y, Z, CS>::kThreads, 2)
+    k_pass2_cl(const Pass2Params p, const int re2) {
+  namespace cg = cooperative_groups;
+  constexpr int NT = ClusterPlane<Y, Z, CS>::kThreads;
+  constexpr int CW = ClusterPlane<Y, Z, CS>::kCW, ZB = ClusterPlane<Y, Z, CS>::kZB;
+  extern __shared__ float2 sm[];
+  cg::cluster_group cl = cg::this_cluster();
+  const int c = (int)cl.block_rank();
+  const Geometry& g = p.g;
+  const int nvz = g.nvz, zlo = g.zlo, shift = Z - nvz, hi_start = Z - (nvz - zlo - 1);
+  const int rb = (nvz + CS - 1) / CS;
+  float2* twy = sm;
+  float2* twz = sm + Y;
+  float2* cols = sm + Y + Z;               // [Z][CW + kPad]; in C: [ZB][Y + kPad]
+  float2* rows = cols + Z * (CW + kPad);   // [rb][Y + kPad]
+
+  const int kx = blockIdx.y, f = blockIdx.z % p.nfield, pair = blockIdx.z / p.nfield;
+  constexpr long long plane = (long long)Z * Y;
+  float2* gplane = p.buf + (((long long)pair * p.nfield + f) * g.nx + kx) * plane;
+
+  // A. own valid rows: copy in the entries the rotation can reach, zeros elsewhere
+  const int i0 = c * rb;
+  const int nown = max(0, min(rb, nvz - i0));
+  for (int v = threadIdx.x; v < nown * Y; v += NT) {
+    const int li = v / Y, y = v - li * Y;
+    const int i = i0 + li;
+    const int z = i <= zlo ? i : i + shift;
+    if (row_in_disk(g, signed_coord(z, Z), signed_coord(y, Y), re2))
+      cp_async8(rows + li * (Y + kPad) + y, gplane + (long long)z * Y + y);
+    else
+      rows[li * (Y + kPad) + y] = make_float2(0.f, 0.f);
+  }
+  for (int i = threadIdx.x; i < Y; i += NT) twy[i] = p.twy[i];
+  for (int i = threadIdx.x; i < Z; i += NT) twz[i] = p.twz[i];
+  cp_async_wait_all();
+  __syncthreads();
+  SmemLines own_rows{rows, Y + kPad, 1};
+  ct_lines<Y, false, NT, kEmax>(nown, twy, own_rows, own_rows, own_rows, true, true);
+  ClusterPeers<CS> prow, pcol;
+#pragma unroll
+  for (int k = 0; k < CS; ++k) {
+    prow.p[k] = cl.map_shared_rank(rows, k);
+    pcol.p[k] = cl.map_shared_rank(cols, k);
+  }
+  cl.sync();                               // every block's rows are transformed
+
+  // B. own columns: z transform (first stage gathers the rows), product, inverse z
+  ClusterRowsSrc<Y, CS> zsrc{prow, c * CW, zlo, hi_start, shift, rb};
+  SmemLines own_cols{cols, 1, CW + kPad};
+  const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + (long long)kx * plane + c * CW;
+  ct_fwd_mul_inv<Z, NT, kEmax>(CW, twz, own_cols, SpectrumOperand{spec, Y}, zsrc, false);
+  cl.sync();                               // every block's columns are final
+
+  // C. own z rows: inverse y transform (first stage gathers the columns), write out
+  ClusterColsSrc<Y, CS> ysrc{pcol, c * ZB};
+  SmemLines out_rows{cols, Y + kPad, 1};
+  constexpr CtPlan PY = ct_plan(Y);
+  ct_first_stage_gather<PY.r[0], true, Y, NT, ZB>(ZB, ysrc, out_rows, ClusterBarrier{});
+  __syncthreads();
+  ct_lines_from<Y, true, NT, kEmax, 1>(ZB, twy, out_rows, out_rows, out_rows, false, true);
+  __syncthreads();
+  float2* gout = gplane + (long long)c * ZB * Y;
+#pragma unroll 4
+  for (int v = threadIdx.x; v < ZB * Y; v += NT) {
+    const int zl = v / Y, y = v - zl * Y;
+    gout[v] = cols[zl * (Y + kPad) + y];
+  }
+}
+
+// Cluster size of the clustered plane pass per fast size (0: one block per
+// plane).  Where one block's plane fits, one block per plane is faster: at
+// 128^3 a two-block cluster ran pass 2 1.6x slower than one 1024-thread block,
+// its distributed-shared-memory reads waiting on the load queue.
+#ifndef PF_CLUSTER_PLANE
+#define PF_CLUSTER_PLANE 0
+#endif
+template <int N>
+struct ClusterOf {
+  static constexpr int kCS = PF_CLUSTER_PLANE;
+};
 
 // ---------------------------------------------------------------------------
 // Pass 3 (fast): inverse x transform, LCC, running max / argmax
@@ -214,7 +373,7 @@ struct TileLines {
   __device__ __forceinline__ void store(int line, int idx, float2 v) const { base[off(line) + idx * ty] = v; }
 };
 
-template <int X>
+template <int X, int NT>
 __device__ __forceinline__ void pass3_prefetch(const float2* __restrict__ base, float2* fld, int ty, int y0, int ny,
                                                int nz, int z) {
   // buf[f][kx][z][y0 .. y0+ty) -> fld[(f*X + kx)*ty .. +ty): 16-byte copies (two rows each)
@@ -223,12 +382,12 @@ __device__ __forceinline__ void pass3_prefetch(const float2* __restrict__ base, 
   const int sh = __ffs(halfty) - 1;
   const long long zrow = (long long)z * ny + y0;
   if (y0 + ty <= ny) {
-    for (int v = threadIdx.x; v < n; v += kThreadsLine) {
+    for (int v = threadIdx.x; v < n; v += NT) {
       const int fk = v >> sh, part = v & (halfty - 1);
       cp_async16(fld + fk * ty + 2 * part, base + (long long)fk * nz * ny + zrow + 2 * part);
     }
   } else {   // last tile of an edge not divisible by ty
-    for (int v = threadIdx.x; v < 3 * X * ty; v += kThreadsLine) {
+    for (int v = threadIdx.x; v < 3 * X * ty; v += NT) {
       const int fk = v / ty, r = v - fk * ty;
       if (y0 + r < ny) cp_async8(fld + fk * ty + r, base + (long long)fk * nz * ny + zrow + r);
       else fld[fk * ty + r] = make_float2(0.f, 0.f);
@@ -236,8 +395,17 @@ __device__ __forceinline__ void pass3_prefetch(const float2* __restrict__ base, 
   }
 }
 
+// Block shape of pass 3: NT threads, two blocks per SM, every voxel of a tile
+// (at most kMaxVoxPerThread * kThreadsLine) owned by one of VPT slots of a thread
+#ifndef PF_PASS3_THREADS
+#define PF_PASS3_THREADS 256
+#endif
+constexpr int kThreadsPass3Ct = PF_PASS3_THREADS;
+constexpr int kVoxPass3Ct = kMaxVoxPerThread * kThreadsLine / kThreadsPass3Ct;
+
 template <int X>
-__global__ void __launch_bounds__(kThreadsLine, 2) k_pass3_ct(const Pass3Params p) {
+__global__ void __launch_bounds__(kThreadsPass3Ct, 2) k_pass3_ct(const Pass3Params p) {
+  constexpr int NT = kThreadsPass3Ct, VPT = kVoxPass3Ct;
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
   float2* tw = sm;
@@ -253,17 +421,17 @@ __global__ void __launch_bounds__(kThreadsLine, 2) k_pass3_ct(const Pass3Params 
   const long long fstride = (long long)X * g.nz * g.ny;
 
   // start the first tile's copies before anything else
-  pass3_prefetch<X>(p.buf, fbuf0, ty, y0, g.ny, g.nz, z);
+  pass3_prefetch<X, NT>(p.buf, fbuf0, ty, y0, g.ny, g.nz, z);
   cp_async_commit();
-  for (int i = threadIdx.x; i < X; i += kThreadsLine) tw[i] = p.twx[i];
+  for (int i = threadIdx.x; i < X; i += NT) tw[i] = p.twx[i];
 
   // voxel v of the tile: row r = v & (ty-1), column x = v >> log2(ty)
-  float best[kMaxVoxPerThread];
-  int brot[kMaxVoxPerThread];
+  float best[VPT];
+  int brot[VPT];
   unsigned int inmask = 0;
 #pragma unroll
-  for (int k = 0; k < kMaxVoxPerThread; ++k) {
-    const int v = threadIdx.x + k * kThreadsLine;
+  for (int k = 0; k < VPT; ++k) {
+    const int v = threadIdx.x + k * NT;
     best[k] = 0.f;
     brot[k] = 0;
     if (v < nvox) {
@@ -281,7 +449,7 @@ __global__ void __launch_bounds__(kThreadsLine, 2) k_pass3_ct(const Pass3Params 
   for (int pair = 0; pair < p.npairs; ++pair) {
     float2* fld = fbuf0 + (pair & 1) * fbuf_stride;
     if (pair + 1 < p.npairs) {
-      pass3_prefetch<X>(p.buf + (long long)(pair + 1) * 3 * fstride, fbuf0 + ((pair + 1) & 1) * fbuf_stride, ty, y0,
+      pass3_prefetch<X, NT>(p.buf + (long long)(pair + 1) * 3 * fstride, fbuf0 + ((pair + 1) & 1) * fbuf_stride, ty, y0,
                         g.ny, g.nz, z);
       cp_async_commit();
       cp_async_wait_group<1>();
@@ -290,13 +458,13 @@ __global__ void __launch_bounds__(kThreadsLine, 2) k_pass3_ct(const Pass3Params 
     }
     __syncthreads();
     TileLines lines{fld, sh, ty, X * ty};
-    ct_lines<X, true, kThreadsLine, kEmax>(3 * ty, tw, lines, lines, lines, true, true);
+    ct_lines<X, true, NT, kEmax>(3 * ty, tw, lines, lines, lines, true, true);
     const long long ra = p.first_rot + 2LL * pair;
     const bool has_b = ra + 1 < p.nrot;
 #pragma unroll
-    for (int k = 0; k < kMaxVoxPerThread; ++k) {
+    for (int k = 0; k < VPT; ++k) {
       if (inmask & (1u << k)) {
-        const int v = threadIdx.x + k * kThreadsLine;
+        const int v = threadIdx.x + k * NT;
         const int r = v & (ty - 1), x = v >> sh;
         const int o = x * ty + r;
         const float2 f0 = fld[o];
@@ -317,8 +485,8 @@ __global__ void __launch_bounds__(kThreadsLine, 2) k_pass3_ct(const Pass3Params 
     __syncthreads();
   }
 #pragma unroll
-  for (int k = 0; k < kMaxVoxPerThread; ++k) {
-    const int v = threadIdx.x + k * kThreadsLine;
+  for (int k = 0; k < VPT; ++k) {
+    const int v = threadIdx.x + k * NT;
     if (v < nvox) {
       const int r = v & (ty - 1), x = v >> sh;
       const int y = y0 + r;
@@ -344,11 +512,31 @@ struct FastSize {
   static void pass1(const Pass1Params& p, int re2, dim3 grid, size_t smem, cudaStream_t s) {
     k_pass1_ct<N><<<grid, kThreadsLine, smem, s>>>(p, re2);
   }
+  // grid: (nx, fields, pairs) planes
   static void pass2(const Pass2Params& p, int re2, dim3 grid, size_t smem, cudaStream_t s) {
+    constexpr int CS = ClusterOf<N>::kCS;
+    if constexpr (CS > 0) {
+      if (p.mode == 0) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(CS, grid.x, grid.y * grid.z);
+        cfg.blockDim = dim3(ClusterPlane<N, N, CS>::kThreads);
+        cfg.dynamicSmemBytes = ClusterPlane<N, N, CS>::smem(p.g.nvz);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = CS;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k_pass2_cl<N, N, CS>, p, re2);   // errors surface in cudaGetLastError
+        return;
+      }
+    }
     k_pass2_ct<N, N><<<grid, PlaneLaunch<N, N>::kThreads, smem, s>>>(p, re2);
   }
   static void pass3(const Pass3Params& p, dim3 grid, size_t smem, cudaStream_t s) {
-    k_pass3_ct<N><<<grid, kThreadsLine, smem, s>>>(p);
+    k_pass3_ct<N><<<grid, kThreadsPass3Ct, smem, s>>>(p);
   }
   template <class K>
   static cudaError_t allow_smem(K kernel, size_t bytes) {
@@ -363,6 +551,10 @@ struct FastSize {
     cudaError_t e = allow_smem(k_pass1_ct<N>, smem_line);
     if (e == cudaSuccess) e = allow_smem(k_pass3_ct<N>, smem_line);
     if (e == cudaSuccess) e = allow_smem(k_pass2_ct<N, N>, smem_plane);
+    constexpr int CS = ClusterOf<N>::kCS;
+    if constexpr (CS > 0) {
+      if (e == cudaSuccess) e = allow_smem(k_pass2_cl<N, N, CS>, ClusterPlane<N, N, CS>::smem(N));
+    }
     return e;
   }
   static FastLaunch table() { return FastLaunch{&pass1, &pass2, &pass3, &set_attrs}; }
