@@ -97,15 +97,22 @@ __device__ __forceinline__ SourcePoint source_point(const RotFixed& R, int cz, i
 // order (((r6 z) + (r3 y)) + (r0 x), no fused multiply-add), so that the nearest
 // voxel agrees with the float64 reference even when the fixed-point
 // representation of the matrix is 2^-33 away from its float64 value.
+// The float64 decision is a separate, never-inlined function: inlined, the
+// compiler evaluates it under a predicate for every point, and GB300 issues
+// float64 at 1/64 of the float32 rate.
+static __device__ __noinline__ int round_f64(const double* __restrict__ rd, int c0, int c1, int c2, int cz, int cy, int cx) {
+  const double v = __dadd_rn(__dadd_rn(__dmul_rn(rd[c2], (double)cz), __dmul_rn(rd[c1], (double)cy)),
+                             __dmul_rn(rd[c0], (double)cx));
+  return (int)round(v);
+}
+
 __device__ __forceinline__ int round_fixed(long long q, const double* __restrict__ rd, int c0, int c1, int c2,
                                            int cz, int cy, int cx) {
   const long long fl = q >> 32;
   const unsigned int frac = (unsigned int)(q & 0xffffffffLL);
   const int dist = (int)(frac - 0x80000000u);
   if (dist > 512 || dist < -512) return (int)fl + (frac > 0x80000000u ? 1 : 0);
-  double v = __dadd_rn(__dadd_rn(__dmul_rn(rd[c2], (double)cz), __dmul_rn(rd[c1], (double)cy)),
-                       __dmul_rn(rd[c0], (double)cx));
-  return (int)round(v);
+  return round_f64(rd, c0, c1, c2, cz, cy, cx);
 }
 
 // 0.32 fixed-point fraction -> float in [0, 1): the top 23 bits become the
