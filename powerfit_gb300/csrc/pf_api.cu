@@ -22,6 +22,7 @@ pf::FastLaunch pf_fast_table_64();
 pf::FastLaunch pf_fast_table_96();
 pf::FastLaunch pf_fast_table_128();
 pf::FastLaunch pf_fast_table_160();
+pf::FastLaunch pf_fast_table_192();
 
 namespace {
 
@@ -295,6 +296,7 @@ bool fast_table(int n, FastLaunch* fl) {
     case 96: *fl = pf_fast_table_96(); return true;
     case 128: *fl = pf_fast_table_128(); return true;
     case 160: *fl = pf_fast_table_160(); return true;
+    case 192: *fl = pf_fast_table_192(); return true;
     default: return false;
   }
 }
@@ -447,7 +449,13 @@ pf_ctx* pf_create(int nz, int ny, int nx, int device, int* status) {
   c->max_smem = prop.sharedMemPerBlockOptin;
   c->split = plane_smem(ny, nz) > c->max_smem;
   c->rmax = std::min(nz, std::min(ny, nx)) / 2;
-  if (nz == ny && ny == nx && !c->split) c->fast = fast_table(nx, &c->fl);
+  if (nz == ny && ny == nx) {
+    FastLaunch fl{};
+    if (fast_table(nx, &fl) && (!c->split || fl.cluster_plane)) {
+      c->fast = true;
+      c->fl = fl;
+    }
+  }
   choose_tiles(c);
   int rc = PF_OK;
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
@@ -671,8 +679,8 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     p2.mode = 0;
     dim3 g2(c->nx, 3, npairs);
     rc = timed_launch(c, 1, [&] {
-      if (c->split) launch_split_pass2(c, g, npairs, 3, 0, nullptr, 1.0f);
-      else if (fast) c->fl.pass2(p2, re2, g2, s2, c->stream);
+      if (fast) c->fl.pass2(p2, re2, g2, s2, c->stream);
+      else if (c->split) launch_split_pass2(c, g, npairs, 3, 0, nullptr, 1.0f);
       else k_pass2<<<g2, kThreadsPlane, s2, c->stream>>>(p2);
     });
     if (rc) return rc;

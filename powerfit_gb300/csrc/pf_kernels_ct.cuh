@@ -251,19 +251,21 @@ struct ClusterBarrier {
 
 template <int Y, int Z, int CS>
 struct ClusterPlane {
-  static constexpr int kThreads = 512;
   static constexpr int kCW = Y / CS;   // columns per block
   static constexpr int kZB = Z / CS;   // z rows per block after the z transform
   static_assert(Y % CS == 0 && Z % CS == 0, "cluster must divide the plane");
   // shared memory: twiddles, column array [Z][CW + kPad], row array [rb][Y + kPad]
-  static size_t smem(int nvz) {
-    const int rb = (nvz + CS - 1) / CS;
-    return ((size_t)Y + Z + (size_t)Z * (kCW + kPad) + (size_t)rb * (Y + kPad)) * sizeof(float2);
+  static constexpr size_t smem(int nvz) {
+    return ((size_t)Y + Z + (size_t)Z * (kCW + kPad) + (size_t)((nvz + CS - 1) / CS) * (Y + kPad)) * sizeof(float2);
   }
+  // two 512-thread blocks per SM where two fit, else one of 1024 threads (64 registers either way)
+  static constexpr bool kTwo = smem(Z) <= 113 * 1024;
+  static constexpr int kThreads = kTwo ? 512 : 1024;
+  static constexpr int kMinBlocks = kTwo ? 2 : 1;
 };
 
 template <int Y, int Z, int CS>
-__global__ void __launch_bounds__(ClusterPlane<Y, Z, CS>::kThreads, 2)
+__global__ void __launch_bounds__(ClusterPlane<Y, Z, CS>::kThreads, ClusterPlane<Y, Z, CS>::kMinBlocks)
     k_pass2_cl(const Pass2Params p, const int re2) {
   namespace cg = cooperative_groups;
   constexpr int NT = ClusterPlane<Y, Z, CS>::kThreads;
@@ -332,16 +334,24 @@ __global__ void __launch_bounds__(ClusterPlane<Y, Z, CS>::kThreads, 2)
   }
 }
 
+// Whether one block holds a whole N x N plane (twiddles, plane, last-stage
+// twiddle table) within the 227 KB a block may use.
+template <int N>
+constexpr bool plane_fits_block() {
+  return ((size_t)2 * N + (size_t)N * (N + kPad) + N) * sizeof(float2) <= 227 * 1024;
+}
+
 // Cluster size of the clustered plane pass per fast size (0: one block per
 // plane).  Where one block's plane fits, one block per plane is faster: at
 // 128^3 a two-block cluster ran pass 2 1.6x slower than one 1024-thread block,
-// its distributed-shared-memory reads waiting on the load queue.
+// its distributed-shared-memory reads waiting on the load queue.  Larger
+// planes (192^2: 296 KB) are shared by four blocks.
 #ifndef PF_CLUSTER_PLANE
 #define PF_CLUSTER_PLANE 0
 #endif
 template <int N>
 struct ClusterOf {
-  static constexpr int kCS = PF_CLUSTER_PLANE;
+  static constexpr int kCS = PF_CLUSTER_PLANE ? PF_CLUSTER_PLANE : (plane_fits_block<N>() ? 0 : 4);
 };
 
 // ---------------------------------------------------------------------------
@@ -505,6 +515,7 @@ struct FastLaunch {
   void (*pass2)(const Pass2Params&, int re2, dim3 grid, size_t smem, cudaStream_t s);
   void (*pass3)(const Pass3Params&, dim3 grid, size_t smem, cudaStream_t s);
   cudaError_t (*set_attrs)(size_t smem_line, size_t smem_plane);
+  bool cluster_plane;   // pass 2 (correlation) runs even where a plane exceeds one block's shared memory
 };
 
 template <int N>
@@ -533,7 +544,8 @@ struct FastSize {
         return;
       }
     }
-    k_pass2_ct<N, N><<<grid, PlaneLaunch<N, N>::kThreads, smem, s>>>(p, re2);
+    // (planes beyond one block take the split path for the target spectra)
+    if constexpr (plane_fits_block<N>()) k_pass2_ct<N, N><<<grid, PlaneLaunch<N, N>::kThreads, smem, s>>>(p, re2);
   }
   static void pass3(const Pass3Params& p, dim3 grid, size_t smem, cudaStream_t s) {
     k_pass3_ct<N><<<grid, kThreadsPass3Ct, smem, s>>>(p);
@@ -550,14 +562,16 @@ struct FastSize {
   static cudaError_t set_attrs(size_t smem_line, size_t smem_plane) {
     cudaError_t e = allow_smem(k_pass1_ct<N>, smem_line);
     if (e == cudaSuccess) e = allow_smem(k_pass3_ct<N>, smem_line);
-    if (e == cudaSuccess) e = allow_smem(k_pass2_ct<N, N>, smem_plane);
+    if constexpr (plane_fits_block<N>()) {
+      if (e == cudaSuccess) e = allow_smem(k_pass2_ct<N, N>, smem_plane);
+    }
     constexpr int CS = ClusterOf<N>::kCS;
     if constexpr (CS > 0) {
       if (e == cudaSuccess) e = allow_smem(k_pass2_cl<N, N, CS>, ClusterPlane<N, N, CS>::smem(N));
     }
     return e;
   }
-  static FastLaunch table() { return FastLaunch{&pass1, &pass2, &pass3, &set_attrs}; }
+  static FastLaunch table() { return FastLaunch{&pass1, &pass2, &pass3, &set_attrs, ClusterOf<N>::kCS > 0}; }
 };
 
 }  // namespace pf
