@@ -8,6 +8,7 @@
 // consecutive lines), so with an odd row stride every access is free of
 // shared-memory bank conflicts whatever the index pattern of the stage.
 #pragma once
+#include <type_traits>
 #include "pf_fft.cuh"
 
 namespace pf {
@@ -292,16 +293,23 @@ constexpr int ct_stage_ns_rev(int n, int stage) {
   return ns;
 }
 
-// Generic stage with an explicit radix (for reversed plans).
-template <int L, bool INV, int NT, int EMAX, int S, class Mid>
-__device__ __forceinline__ void ct_rev_from(int nlines, const float2* __restrict__ tw, const Mid& mid) {
+// Stages S .. nst-1 of the reversed plan, in place in `mid`; the last one
+// stores to `dst` instead when `kToDst` (a different memory: no barrier
+// between its loads and stores, none after it).
+template <int L, bool INV, int NT, int EMAX, int S, bool kToDst = false, class Mid, class Dst = Mid>
+__device__ __forceinline__ void ct_rev_from(int nlines, const float2* __restrict__ tw, const Mid& mid,
+                                            const Dst& dst = Dst{}) {
   constexpr CtPlan Q = ct_plan_rev(L);
   if constexpr (S < Q.nst) {
     constexpr int R = Q.r[S];
     constexpr int NS = ct_stage_ns_rev(L, S);
-    ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, mid, mid, true);
-    __syncthreads();
-    ct_rev_from<L, INV, NT, EMAX, S + 1>(nlines, tw, mid);
+    if constexpr (kToDst && S == Q.nst - 1) {
+      ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, mid, dst, false);
+    } else {
+      ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, mid, mid, true);
+      __syncthreads();
+      ct_rev_from<L, INV, NT, EMAX, S + 1, kToDst>(nlines, tw, mid, dst);
+    }
   }
 }
 
@@ -313,9 +321,13 @@ __device__ __forceinline__ void ct_rev_from(int nlines, const float2* __restrict
 //
 // The forward's first stage reads `src` (by default `mid` itself); `src_alias`
 // says whether it shares memory with `mid`.
-template <int L, int NT, int EMAX, class Mid, class Mul, class Src = Mid>
+//
+// With a `Dst` other than `void`, the inverse's last stage stores to `dst`
+// (the plan must have at least two stages) and no barrier follows it.
+template <int L, int NT, int EMAX, class Mid, class Mul, class Src = Mid, class Dst = void>
 __device__ __forceinline__ void ct_fwd_mul_inv(int nlines, const float2* __restrict__ tw, const Mid& mid,
-                                               const Mul& mul, const Src& src, bool src_alias) {
+                                               const Mul& mul, const Src& src, bool src_alias,
+                                               const Dst* dstp = nullptr) {
   constexpr CtPlan P = ct_plan(L);
   constexpr int RL = P.r[P.nst - 1];
   constexpr int NB = L / RL;
@@ -367,7 +379,12 @@ __device__ __forceinline__ void ct_fwd_mul_inv(int nlines, const float2* __restr
     __syncthreads();
   }
   // inverse stages 1 .. nst-1 of the reversed plan
-  ct_rev_from<L, true, NT, EMAX, 1>(nlines, tw, mid);
+  if constexpr (std::is_void<Dst>::value) {
+    ct_rev_from<L, true, NT, EMAX, 1>(nlines, tw, mid);
+  } else {
+    static_assert(P.nst >= 2, "the last inverse stage must not be the fused one");
+    ct_rev_from<L, true, NT, EMAX, 1, true>(nlines, tw, mid, *dstp);
+  }
 }
 
 }  // namespace pf

@@ -193,60 +193,73 @@ __global__ void __launch_bounds__(PlaneLaunch<Y, Z>::kThreads, PlaneLaunch<Y, Z>
 
 // ---------------------------------------------------------------------------
 // Pass 2 (fast, clustered): the plane of one (pair, field, kx) shared by a
-// cluster of CS blocks, each holding 1/CS of it, so that a 128 x 128 plane
-// leaves room for two blocks per SM.
+// cluster of CS blocks, for planes larger than one block's shared memory.
+// Every exchange is a push: the last stage of a transform stores its outputs
+// straight into the shared memory of the block that owns them next
+// (st.shared::cluster), so no block ever waits on a remote load.
 //
-//   A. block c copies in and y-transforms its share of the valid z rows
-//      (rb = ceil(nvz / CS) rows from valid row c*rb on);
-//   B. it z-transforms its CW = Y/CS columns: the first stage reads the rows
-//      from every block's shared memory (distributed shared memory), the
-//      product and the inverse z run in its own column array;
-//   C. it inverse-y-transforms its ZB = Z/CS z rows: the first stage reads
-//      the columns from every block, and, after a cluster barrier, stores
-//      into its own column array (as rows); then it writes its rows out.
+//   A. block c copies in its share of the valid z rows (rb = ceil(nvz / CS)
+//      rows from valid row c*rb on) and y-transforms them; the last y stage
+//      stores column ky into the column array of block ky / CW (CW = Y/CS);
+//   B. block c z-transforms its CW columns, multiplies, inverse-z-transforms;
+//      the last inverse stage stores row z into the row array of block z / ZB
+//      (ZB = Z/CS);
+//   C. block c inverse-y-transforms its ZB rows, the last stage straight to
+//      the buffer in global memory.
 //
-// Three cluster barriers order the exchange: rows complete before B, columns
-// complete before C, every read of C done before C's stores.  No block reads
-// another's memory after the last one, so a block may exit right after it.
+// Cluster barriers (release / acquire) order the pushes: one before A's
+// pushes (every block of the cluster is running), one after them, one after
+// B's.  The row array holds A's input rows and C's rows: peers push into it
+// only after the second barrier, when A is done with it.  After the third
+// barrier no block touches another's memory, so every block may exit.
 // ---------------------------------------------------------------------------
 template <int CS>
-struct ClusterPeers {  // the same shared-memory array in each block of the cluster
-  float2* p[CS];
-  __device__ __forceinline__ float2* get(int r) const {
-    float2* q = p[0];
+struct ClusterBases {  // shared::cluster addresses of one array in each block of the cluster
+  unsigned int a[CS];
+  __device__ __forceinline__ unsigned int get(int r) const {
+    unsigned int q = a[0];
 #pragma unroll
-    for (int k = 1; k < CS; ++k) q = (r == k) ? p[k] : q;
+    for (int k = 1; k < CS; ++k) q = (r == k) ? a[k] : q;
     return q;
   }
 };
 
-template <int Y, int CS>
-struct ClusterRowsSrc {  // z transform input: line = own column (ky - ky0), idx = z
-  ClusterPeers<CS> rows;  // valid rows, rb per block, row stride Y + kPad
-  int ky0, zlo, hi_start, shift, rb;
-  __device__ __forceinline__ float2 load(int line, int z) const {
-    if (z > zlo && z < hi_start) return make_float2(0.f, 0.f);   // plane the rotation cannot reach
-    const int i = z <= zlo ? z : z - shift;                        // valid-row index
-    int owner = 0;
-#pragma unroll
-    for (int k = 1; k < CS; ++k) owner += (i >= k * rb) ? 1 : 0;
-    return rows.get(owner)[(i - owner * rb) * (Y + kPad) + ky0 + line];
-  }
-};
+__device__ __forceinline__ unsigned int cluster_addr(const void* smem, int rank) {
+  unsigned int d;
+  const unsigned int a = (unsigned int)__cvta_generic_to_shared(smem);
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(rank));
+  return d;
+}
 
-template <int Y, int CS>
-struct ClusterColsSrc {  // inverse y input: line = own z row (z - z0), idx = ky
+__device__ __forceinline__ void st_cluster(unsigned int addr, float2 v) {
+  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(addr), "f"(v.x), "f"(v.y) : "memory");
+}
+
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+template <int Y, int Z, int CS>
+struct PushToColumns {  // A's last stage: line = own valid row, idx = ky -> column array of block ky / CW
   static constexpr int CW = Y / CS;
-  ClusterPeers<CS> cols;  // column arrays [z][CW + kPad]
-  int z0;
-  __device__ __forceinline__ float2 load(int line, int ky) const {
+  ClusterBases<CS> cols;
+  int i0, zlo, shift;
+  __device__ __forceinline__ void store(int line, int ky, float2 v) const {
+    const int i = i0 + line;
+    const int z = i <= zlo ? i : i + shift;
     const int owner = ky / CW;
-    return cols.get(owner)[(z0 + line) * (CW + kPad) + ky - owner * CW];
+    st_cluster(cols.get(owner) + (unsigned int)((z * (CW + kPad) + ky - owner * CW) * sizeof(float2)), v);
   }
 };
 
-struct ClusterBarrier {
-  __device__ __forceinline__ void operator()() const { cooperative_groups::this_cluster().sync(); }
+template <int Y, int Z, int CS>
+struct PushToRows {  // B's last stage: line = own column (ky - ky0), idx = z -> row array of block z / ZB
+  static constexpr int ZB = Z / CS;
+  ClusterBases<CS> rows;
+  int ky0;
+  __device__ __forceinline__ void store(int line, int z, float2 v) const {
+    const int owner = z / ZB;
+    st_cluster(rows.get(owner) + (unsigned int)(((z - owner * ZB) * (Y + kPad) + ky0 + line) * sizeof(float2)), v);
+  }
 };
 
 template <int Y, int Z, int CS>
@@ -254,9 +267,12 @@ struct ClusterPlane {
   static constexpr int kCW = Y / CS;   // columns per block
   static constexpr int kZB = Z / CS;   // z rows per block after the z transform
   static_assert(Y % CS == 0 && Z % CS == 0, "cluster must divide the plane");
-  // shared memory: twiddles, column array [Z][CW + kPad], row array [rb][Y + kPad]
+  // shared memory: twiddles (y, z, last-stage y table), column array [Z][CW + kPad],
+  // row array [max(rb, ZB)][Y + kPad]
   static constexpr size_t smem(int nvz) {
-    return ((size_t)Y + Z + (size_t)Z * (kCW + kPad) + (size_t)((nvz + CS - 1) / CS) * (Y + kPad)) * sizeof(float2);
+    const int rb = (nvz + CS - 1) / CS;
+    const int nr = rb > kZB ? rb : kZB;
+    return ((size_t)2 * Y + Z + (size_t)Z * (kCW + kPad) + (size_t)nr * (Y + kPad)) * sizeof(float2);
   }
   // two 512-thread blocks per SM where two fit, else one of 1024 threads (64 registers either way)
   static constexpr bool kTwo = smem(Z) <= 113 * 1024;
@@ -271,21 +287,23 @@ __global__ void __launch_bounds__(ClusterPlane<Y, Z, CS>::kThreads, ClusterPlane
   constexpr int NT = ClusterPlane<Y, Z, CS>::kThreads;
   constexpr int CW = ClusterPlane<Y, Z, CS>::kCW, ZB = ClusterPlane<Y, Z, CS>::kZB;
   extern __shared__ float2 sm[];
-  cg::cluster_group cl = cg::this_cluster();
-  const int c = (int)cl.block_rank();
+  const int c = (int)cg::this_cluster().block_rank();
+  cluster_arrive();                        // this block is running (waited on before the first push)
   const Geometry& g = p.g;
   const int nvz = g.nvz, zlo = g.zlo, shift = Z - nvz, hi_start = Z - (nvz - zlo - 1);
   const int rb = (nvz + CS - 1) / CS;
   float2* twy = sm;
   float2* twz = sm + Y;
-  float2* cols = sm + Y + Z;               // [Z][CW + kPad]; in C: [ZB][Y + kPad]
-  float2* rows = cols + Z * (CW + kPad);   // [rb][Y + kPad]
+  float2* tly = sm + Y + Z;                // last inverse-y stage twiddles, [r][j]
+  float2* cols = sm + 2 * Y + Z;           // [Z][CW + kPad]
+  float2* rows = cols + Z * (CW + kPad);   // A: [rb][Y + kPad] (own valid rows); C: [ZB][Y + kPad]
 
   const int kx = blockIdx.y, f = blockIdx.z % p.nfield, pair = blockIdx.z / p.nfield;
   constexpr long long plane = (long long)Z * Y;
   float2* gplane = p.buf + (((long long)pair * p.nfield + f) * g.nx + kx) * plane;
 
-  // A. own valid rows: copy in the entries the rotation can reach, zeros elsewhere
+  // A. own valid rows: the entries the rotation can reach, zeros elsewhere;
+  // zeros in the column array's rows outside the valid planes (no block pushes those)
   const int i0 = c * rb;
   const int nown = max(0, min(rb, nvz - i0));
   for (int v = threadIdx.x; v < nown * Y; v += NT) {
@@ -297,41 +315,40 @@ __global__ void __launch_bounds__(ClusterPlane<Y, Z, CS>::kThreads, ClusterPlane
     else
       rows[li * (Y + kPad) + y] = make_float2(0.f, 0.f);
   }
+  for (int v = threadIdx.x; v < (hi_start - zlo - 1) * CW; v += NT) {
+    const int zi = v / CW, col = v - zi * CW;
+    cols[(zlo + 1 + zi) * (CW + kPad) + col] = make_float2(0.f, 0.f);
+  }
   for (int i = threadIdx.x; i < Y; i += NT) twy[i] = p.twy[i];
   for (int i = threadIdx.x; i < Z; i += NT) twz[i] = p.twz[i];
-  cp_async_wait_all();
-  __syncthreads();
-  SmemLines own_rows{rows, Y + kPad, 1};
-  ct_lines<Y, false, NT, kEmax>(nown, twy, own_rows, own_rows, own_rows, true, true);
-  ClusterPeers<CS> prow, pcol;
+  ct_last_twiddles<Y, NT>(p.twy, tly);
+  ClusterBases<CS> bcols, brows;
 #pragma unroll
   for (int k = 0; k < CS; ++k) {
-    prow.p[k] = cl.map_shared_rank(rows, k);
-    pcol.p[k] = cl.map_shared_rank(cols, k);
+    bcols.a[k] = cluster_addr(cols, k);
+    brows.a[k] = cluster_addr(rows, k);
   }
-  cl.sync();                               // every block's rows are transformed
+  cp_async_wait_all();
+  __syncthreads();
+  cluster_wait();                          // every block of the cluster is running
+  SmemLines own_rows{rows, Y + kPad, 1};
+  PushToColumns<Y, Z, CS> to_cols{bcols, i0, zlo, shift};
+  ct_lines<Y, false, NT, kEmax>(nown, twy, own_rows, own_rows, to_cols, true, false);
+  cluster_arrive();
+  cluster_wait();                          // every column array is complete
 
-  // B. own columns: z transform (first stage gathers the rows), product, inverse z
-  ClusterRowsSrc<Y, CS> zsrc{prow, c * CW, zlo, hi_start, shift, rb};
+  // B. own columns: z transform, product, inverse z; the last stage pushes rows
   SmemLines own_cols{cols, 1, CW + kPad};
   const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + (long long)kx * plane + c * CW;
-  ct_fwd_mul_inv<Z, NT, kEmax>(CW, twz, own_cols, SpectrumOperand{spec, Y}, zsrc, false);
-  cl.sync();                               // every block's columns are final
+  PushToRows<Y, Z, CS> to_rows{brows, c * CW};
+  ct_fwd_mul_inv<Z, NT, kEmax>(CW, twz, own_cols, SpectrumOperand{spec, Y}, own_cols, true, &to_rows);
+  cluster_arrive();
+  cluster_wait();                          // every row array is complete; no more remote stores
 
-  // C. own z rows: inverse y transform (first stage gathers the columns), write out
-  ClusterColsSrc<Y, CS> ysrc{pcol, c * ZB};
-  SmemLines out_rows{cols, Y + kPad, 1};
-  constexpr CtPlan PY = ct_plan(Y);
-  ct_first_stage_gather<PY.r[0], true, Y, NT, ZB>(ZB, ysrc, out_rows, ClusterBarrier{});
-  __syncthreads();
-  ct_lines_from<Y, true, NT, kEmax, 1>(ZB, twy, out_rows, out_rows, out_rows, false, true);
-  __syncthreads();
-  float2* gout = gplane + (long long)c * ZB * Y;
-#pragma unroll 4
-  for (int v = threadIdx.x; v < ZB * Y; v += NT) {
-    const int zl = v / Y, y = v - zl * Y;
-    gout[v] = cols[zl * (Y + kPad) + y];
-  }
+  // C. own z rows: inverse y, the last stage straight to the buffer
+  SmemLines out_rows{rows, Y + kPad, 1};
+  ct_head_inplace<Y, true, NT, kEmax, 0>(ZB, twy, out_rows);
+  ct_last_stage_out<Y, true, NT>(ZB, tly, out_rows, GlobalRows{gplane + (long long)c * ZB * Y, Y});
 }
 
 // Whether one block holds a whole N x N plane (twiddles, plane, last-stage
