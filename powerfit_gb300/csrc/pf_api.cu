@@ -109,6 +109,8 @@ struct pf_ctx {
   float2* spec = nullptr;          // [2][kx][kz][ky]
   float* lcc = nullptr;
   int* rot = nullptr;
+  float* part_lcc = nullptr;        // fast pass 3 split over two blocks per tile: best of the later pairs
+  int* part_rot = nullptr;
   float2* buf = nullptr;
   long long buf_pairs = 0;
   RotFixed* rots = nullptr;
@@ -123,6 +125,7 @@ struct pf_ctx {
   bool have_target = false, have_template = false;
   int pairs = 1, ty1 = 16, ty3 = 16;
   size_t max_smem = 0;
+  int num_sms = 0;
   bool fast = false;                 // compile-time-specialised kernels for this grid
   bool split = false;                // (z, y) plane larger than shared memory: pass 2 in three steps
   FastLaunch fl{};
@@ -194,6 +197,18 @@ void choose_tiles(pf_ctx* c) {
   const long long per_pair = 3LL * c->N * (long long)sizeof(float2);
   long long p = (64LL << 20) / per_pair;
   c->pairs = (int)std::max(1LL, std::min(16LL, p));
+}
+
+// best of the later half of a batch's pairs (fast pass 3 split over two
+// blocks per tile); zero outside the lcc mask, which no block writes
+int ensure_part(pf_ctx* c) {
+  if (c->part_lcc) return PF_OK;
+  int rc = alloc(c, (void**)&c->part_lcc, c->N * sizeof(float));
+  if (!rc) rc = alloc(c, (void**)&c->part_rot, c->N * sizeof(int));
+  if (rc) return rc;
+  PF_CUDA(c, cudaMemsetAsync(c->part_lcc, 0, c->N * sizeof(float), c->stream));
+  PF_CUDA(c, cudaMemsetAsync(c->part_rot, 0, c->N * sizeof(int), c->stream));
+  return PF_OK;
 }
 
 int ensure_buf(pf_ctx* c, int pairs) {
@@ -447,6 +462,7 @@ pf_ctx* pf_create(int nz, int ny, int nx, int device, int* status) {
   cudaDeviceProp prop;
   cudaGetDeviceProperties(&prop, device);
   c->max_smem = prop.sharedMemPerBlockOptin;
+  c->num_sms = prop.multiProcessorCount;
   c->split = plane_smem(ny, nz) > c->max_smem;
   c->rmax = std::min(nz, std::min(ny, nx)) / 2;
   if (nz == ny && ny == nx) {
@@ -502,7 +518,7 @@ int pf_destroy(pf_ctx* c) {
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   c->own_stream = nullptr;
   void* ptrs[] = {c->twx, c->twy, c->twz, c->tmpl, c->mask, c->lcc_mask, c->spec, c->lcc, c->rot, c->buf, c->rots, c->rotd,
-                  c->rows_reach, c->rows_full, c->tmpl_pairs};
+                  c->rows_reach, c->rows_full, c->tmpl_pairs, c->part_lcc, c->part_rot};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete c;
@@ -687,10 +703,31 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     Pass3Params p3{g, c->px, c->twx, c->buf, npairs, r0, end, rot_offset, c->lcc_mask, c->norm_factor,
                    c->lcc, c->rot, ty3, (flags & PF_FLAG_FP64_NORM) ? 1 : 0};
     dim3 g3(c->nz, (c->ny + ty3 - 1) / ty3, 1);
+    // Each pass-3 block runs through all pairs of the batch, so a grid of a
+    // few waves leaves much of its last wave idle; splitting the pairs over
+    // two blocks per tile (merged afterwards) evens the waves out.
+    if (fast && npairs >= 4 && c->num_sms > 0) {
+      const double slots = 2.0 * c->num_sms;   // two pass-3 blocks per SM
+      auto eff = [&](double blocks) { const double w = blocks / slots; return w / std::ceil(w); };
+      const double tiles = (double)g3.x * g3.y;
+      if (eff(2 * tiles) > eff(tiles) + 0.05) {
+        rc = ensure_part(c);
+        if (rc) return rc;
+        g3.z = 2;
+        p3.part_lcc = c->part_lcc;
+        p3.part_rot = c->part_rot;
+      }
+    }
     const size_t s3f = pass3_smem(c->nx, ty3, npairs > 1 ? 2 : 1);
     rc = timed_launch(c, 2, [&] {
-      if (fast) c->fl.pass3(p3, g3, s3f, c->stream);
-      else k_pass3<<<g3, kThreadsLine, s3, c->stream>>>(p3);
+      if (fast) {
+        c->fl.pass3(p3, g3, s3f, c->stream);
+        if (g3.z == 2)
+          k_combine<<<(unsigned)std::min<long long>((c->N + 255) / 256, 4 * 1024), 256, 0, c->stream>>>(
+              c->part_lcc, c->part_rot, 0, c->lcc, c->rot, c->N);
+      } else {
+        k_pass3<<<g3, kThreadsLine, s3, c->stream>>>(p3);
+      }
     });
     if (rc) return rc;
   }

@@ -497,6 +497,11 @@ struct Pass3Params {
   int* __restrict__ rot;       // running argmax
   int ty;
   int fp64;                    // 1: variance and LCC in float64
+  // fast path with gridDim.z == 2: blocks with blockIdx.z == 1 take the later
+  // half of the pairs, starting from 0, and keep their best in these arrays
+  // (merged into lcc / rot afterwards, the earlier half winning ties)
+  float* __restrict__ part_lcc = nullptr;
+  int* __restrict__ part_rot = nullptr;
 };
 
 struct GlobalRowsLoad {  // line = f*ty + r, idx = kx: buf[f][kx][z][y0 + r]

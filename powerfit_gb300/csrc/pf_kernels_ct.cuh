@@ -379,8 +379,12 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // Shared-memory bytes of pass 3 for `nbuf` tile buffers ([3][X][ty] complex).
+// float2 slots holding the list of a tile's voxels inside the lcc mask (one 16-bit entry each)
+__host__ __device__ inline int pass3_list_slots(int X, int ty) { return (ty * X * 2 + 7) / 8; }
+
+// twiddles, the voxel list, nbuf tile buffers
 __host__ __device__ inline size_t pass3_smem(int X, int ty, int nbuf) {
-  return ((size_t)X + (size_t)nbuf * 3 * ty * X) * sizeof(float2);
+  return ((size_t)X + pass3_list_slots(X, ty) + (size_t)nbuf * 3 * ty * X) * sizeof(float2);
 }
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -435,9 +439,10 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, 2) k_pass3_ct(const Pass3Para
   constexpr int NT = kThreadsPass3Ct, VPT = kVoxPass3Ct;
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
-  float2* tw = sm;
-  float2* fbuf0 = sm + X;
   const int ty = p.ty;                      // a power of two >= 2 on this path
+  float2* tw = sm;
+  unsigned short* s_list = reinterpret_cast<unsigned short*>(sm + X);
+  float2* fbuf0 = sm + X + pass3_list_slots(X, ty);
   const int sh = __ffs(ty) - 1;
   const int fbuf_stride = 3 * ty * X;
 
@@ -447,37 +452,80 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, 2) k_pass3_ct(const Pass3Para
   const long long zoff = (long long)z * g.ny * X;
   const long long fstride = (long long)X * g.nz * g.ny;
 
+  // pairs of this block: all, or one half (blockIdx.z) when the pairs are split over two blocks
+  const int half = (p.npairs + 1) >> 1;
+  const int pb = (gridDim.z == 1 || blockIdx.z == 0) ? 0 : half;
+  const int pe = gridDim.z == 1 ? p.npairs : (blockIdx.z == 0 ? half : p.npairs);
+
   // start the first tile's copies before anything else
-  pass3_prefetch<X, NT>(p.buf, fbuf0, ty, y0, g.ny, g.nz, z);
+  if (pb < pe) pass3_prefetch<X, NT>(p.buf + (long long)pb * 3 * fstride, fbuf0, ty, y0, g.ny, g.nz, z);
   cp_async_commit();
   for (int i = threadIdx.x; i < X; i += NT) tw[i] = p.twx[i];
 
-  // voxel v of the tile: row r = v & (ty-1), column x = v >> log2(ty)
-  float best[VPT];
-  int brot[VPT];
+  // voxel v of the tile: row r = v & (ty-1), column x = v >> log2(ty).  The
+  // voxels inside the lcc mask (the only ones whose best value can change)
+  // are listed in order; thread t keeps the running best of list entries
+  // m = t + k NT in registers.
   unsigned int inmask = 0;
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
     const int v = threadIdx.x + k * NT;
+    if (v < nvox) {
+      const int y = y0 + (v & (ty - 1));
+      if (y < g.ny && p.lcc_mask[zoff + (long long)y * X + (v >> sh)]) inmask |= 1u << k;
+    }
+  }
+  __shared__ int s_warp[NT / 32 + 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int cnt = __popc(inmask);
+  int incl = cnt;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += t;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int w = 0; w < NT / 32; ++w) {
+      const int t = s_warp[w];
+      s_warp[w] = acc;
+      acc += t;
+    }
+    s_warp[NT / 32] = acc;
+  }
+  __syncthreads();
+  {
+    int pos = s_warp[warp] + incl - cnt;
+#pragma unroll
+    for (int k = 0; k < VPT; ++k)
+      if (inmask & (1u << k)) s_list[pos++] = (unsigned short)(threadIdx.x + k * NT);
+  }
+  __syncthreads();
+  const int total = s_warp[NT / 32];
+  float* __restrict__ out_lcc = blockIdx.z == 0 ? p.lcc : p.part_lcc;
+  int* __restrict__ out_rot = blockIdx.z == 0 ? p.rot : p.part_rot;
+  float best[VPT];
+  int brot[VPT];
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    const int m = threadIdx.x + k * NT;
     best[k] = 0.f;
     brot[k] = 0;
-    if (v < nvox) {
-      const int r = v & (ty - 1), x = v >> sh;
-      const int y = y0 + r;
-      if (y < g.ny) {
-        const long long gi = zoff + (long long)y * X + x;
-        best[k] = p.lcc[gi];
-        brot[k] = p.rot[gi];
-        if (p.lcc_mask[gi]) inmask |= 1u << k;
-      }
+    if (m < total && blockIdx.z == 0) {
+      const int v = s_list[m];
+      const long long gi = zoff + (long long)(y0 + (v & (ty - 1))) * X + (v >> sh);
+      best[k] = p.lcc[gi];
+      brot[k] = p.rot[gi];
     }
   }
 
-  for (int pair = 0; pair < p.npairs; ++pair) {
-    float2* fld = fbuf0 + (pair & 1) * fbuf_stride;
-    if (pair + 1 < p.npairs) {
-      pass3_prefetch<X, NT>(p.buf + (long long)(pair + 1) * 3 * fstride, fbuf0 + ((pair + 1) & 1) * fbuf_stride, ty, y0,
-                        g.ny, g.nz, z);
+  for (int pair = pb; pair < pe; ++pair) {
+    float2* fld = fbuf0 + ((pair - pb) & 1) * fbuf_stride;
+    if (pair + 1 < pe) {
+      pass3_prefetch<X, NT>(p.buf + (long long)(pair + 1) * 3 * fstride, fbuf0 + ((pair + 1 - pb) & 1) * fbuf_stride,
+                            ty, y0, g.ny, g.nz, z);
       cp_async_commit();
       cp_async_wait_group<1>();
     } else {
@@ -490,8 +538,9 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, 2) k_pass3_ct(const Pass3Para
     const bool has_b = ra + 1 < p.nrot;
 #pragma unroll
     for (int k = 0; k < VPT; ++k) {
-      if (inmask & (1u << k)) {
-        const int v = threadIdx.x + k * NT;
+      const int m = threadIdx.x + k * NT;
+      if (m < total) {
+        const int v = s_list[m];
         const int r = v & (ty - 1), x = v >> sh;
         const int o = x * ty + r;
         const float2 f0 = fld[o];
@@ -513,15 +562,12 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, 2) k_pass3_ct(const Pass3Para
   }
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
-    const int v = threadIdx.x + k * NT;
-    if (v < nvox) {
-      const int r = v & (ty - 1), x = v >> sh;
-      const int y = y0 + r;
-      if (y < g.ny) {
-        const long long gi = zoff + (long long)y * X + x;
-        p.lcc[gi] = best[k];
-        p.rot[gi] = brot[k];
-      }
+    const int m = threadIdx.x + k * NT;
+    if (m < total) {
+      const int v = s_list[m];
+      const long long gi = zoff + (long long)(y0 + (v & (ty - 1))) * X + (v >> sh);
+      out_lcc[gi] = best[k];
+      out_rot[gi] = brot[k];
     }
   }
 }
