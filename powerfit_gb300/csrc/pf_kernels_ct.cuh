@@ -432,7 +432,7 @@ __device__ __forceinline__ void pass3_prefetch(const float2* __restrict__ base, 
 #define PF_PASS3_THREADS 256
 #endif
 constexpr int kThreadsPass3Ct = PF_PASS3_THREADS;
-constexpr int kVoxPass3Ct = kMaxVoxPerThread * kThreadsLine / kThreadsPass3Ct;
+constexpr int kVoxPass3Ct = (kMaxVoxPerThread * kThreadsLine + kThreadsPass3Ct - 1) / kThreadsPass3Ct;
 
 template <int X>
 __global__ void __launch_bounds__(kThreadsPass3Ct, 2) k_pass3_ct(const Pass3Params p) {
