@@ -133,7 +133,11 @@ struct pf_ctx {
   double ms[3] = {0, 0, 0};
   long long launches[3] = {0, 0, 0};
   std::vector<cudaEvent_t> ev_pool;
-  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  struct Pending {
+    int which, kernels;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;      // profiled launches whose events are not read yet
   char err[512] = "";
 };
 
@@ -253,16 +257,17 @@ cudaEvent_t get_event(pf_ctx* c) {
 void collect_events(pf_ctx* c) {
   for (auto& pe : c->pending) {
     float ms = 0.f;
-    if (cudaEventElapsedTime(&ms, pe.second.first, pe.second.second) == cudaSuccess) {
-      c->ms[pe.first] += ms;
-      c->launches[pe.first] += 1;
+    if (cudaEventElapsedTime(&ms, pe.a, pe.b) == cudaSuccess) {
+      c->ms[pe.which] += ms;
+      c->launches[pe.which] += pe.kernels;
     }
-    c->ev_pool.push_back(pe.second.first);
-    c->ev_pool.push_back(pe.second.second);
+    c->ev_pool.push_back(pe.a);
+    c->ev_pool.push_back(pe.b);
   }
   c->pending.clear();
 }
 
+// `launch()` issues the kernels of one pass and returns how many it launched
 template <class Launch>
 int timed_launch(pf_ctx* c, int which, Launch&& launch) {
   cudaEvent_t a = nullptr, b = nullptr;
@@ -271,12 +276,12 @@ int timed_launch(pf_ctx* c, int which, Launch&& launch) {
     b = get_event(c);
     cudaEventRecord(a, c->stream);
   }
-  launch();
+  const int kernels = launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(c, PF_E_CUDA, "kernel launch (pass %d) failed: %s", which + 1, cudaGetErrorString(e));
   if (c->profiling) {
     cudaEventRecord(b, c->stream);
-    c->pending.push_back({which, {a, b}});
+    c->pending.push_back({which, kernels, a, b});
   }
   return PF_OK;
 }
@@ -672,13 +677,14 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
                    full ? c->rows_full : c->rows_reach, full ? c->nrows_full : c->nrows_reach};
     rc = timed_launch(c, 0, [&] {
       if (fast) {
-        if (p1.nrows > 0) {
-          dim3 g1((p1.nrows + ty1 - 1) / ty1, 1, npairs);
-          c->fl.pass1(p1, re2, g1, s1, c->stream);
-        }
+        if (p1.nrows == 0) return 0;
+        dim3 g1((p1.nrows + ty1 - 1) / ty1, 1, npairs);
+        c->fl.pass1(p1, re2, g1, s1, c->stream);
+        return 1;
       } else {
         dim3 g1(g.nvz, (c->ny + ty1 - 1) / ty1, npairs);
         k_pass1<<<g1, kThreadsLine, s1, c->stream>>>(p1);
+        return 1;
       }
     });
     if (rc) return rc;
@@ -695,9 +701,16 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     p2.mode = 0;
     dim3 g2(c->nx, 3, npairs);
     rc = timed_launch(c, 1, [&] {
-      if (fast) c->fl.pass2(p2, re2, g2, s2, c->stream);
-      else if (c->split) launch_split_pass2(c, g, npairs, 3, 0, nullptr, 1.0f);
-      else k_pass2<<<g2, kThreadsPlane, s2, c->stream>>>(p2);
+      if (fast) {
+        c->fl.pass2(p2, re2, g2, s2, c->stream);
+        return 1;
+      }
+      if (c->split) {
+        launch_split_pass2(c, g, npairs, 3, 0, nullptr, 1.0f);   // rows, columns, rows
+        return 3;
+      }
+      k_pass2<<<g2, kThreadsPlane, s2, c->stream>>>(p2);
+      return 1;
     });
     if (rc) return rc;
     Pass3Params p3{g, c->px, c->twx, c->buf, npairs, r0, end, rot_offset, c->lcc_mask, c->norm_factor,
@@ -722,12 +735,13 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     rc = timed_launch(c, 2, [&] {
       if (fast) {
         c->fl.pass3(p3, g3, s3f, c->stream);
-        if (g3.z == 2)
-          k_combine<<<(unsigned)std::min<long long>((c->N + 255) / 256, 4 * 1024), 256, 0, c->stream>>>(
-              c->part_lcc, c->part_rot, 0, c->lcc, c->rot, c->N);
-      } else {
-        k_pass3<<<g3, kThreadsLine, s3, c->stream>>>(p3);
+        if (g3.z != 2) return 1;
+        k_combine<<<(unsigned)std::min<long long>((c->N + 255) / 256, 4 * 1024), 256, 0, c->stream>>>(
+            c->part_lcc, c->part_rot, 0, c->lcc, c->rot, c->N);
+        return 2;
       }
+      k_pass3<<<g3, kThreadsLine, s3, c->stream>>>(p3);
+      return 1;
     });
     if (rc) return rc;
   }
