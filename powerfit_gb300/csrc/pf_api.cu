@@ -184,6 +184,11 @@ struct DeviceGuard {
   }
 };
 
+// most voxels a pass-3 tile may hold on this context's path
+long long max_vox3(const pf_ctx* c) {
+  return c->fast ? (long long)kMaxVoxPass3Fast : (long long)kMaxVoxPerThread * kThreadsLine;
+}
+
 void choose_tiles(pf_ctx* c) {
   const int X = c->nx;
   int ty = 16;
@@ -194,7 +199,7 @@ void choose_tiles(pf_ctx* c) {
   // a power of two (>= 2 on the fast path, whose pass 3 copies two rows per 16 bytes)
   const int ty3_min = c->fast ? 2 : 1;
   int ty3 = 16;
-  while (ty3 > ty3_min && (long long)ty3 * X > (long long)kMaxVoxPerThread * kThreadsLine) ty3 /= 2;
+  while (ty3 > ty3_min && (long long)ty3 * X > max_vox3(c)) ty3 /= 2;
   while (ty3 > ty3_min && (long long)c->nz * ((c->ny + ty3 - 1) / ty3) < 4 * 152) ty3 /= 2;
   c->ty3 = ty3;
   // pairs per batch: intermediate spectra of one batch <= 64 MiB (L2-sized), at least 1, at most 16
@@ -720,7 +725,7 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     // few waves leaves much of its last wave idle; splitting the pairs over
     // two blocks per tile (merged afterwards) evens the waves out.
     if (fast && npairs >= 4 && c->num_sms > 0) {
-      const double slots = 2.0 * c->num_sms;   // two pass-3 blocks per SM
+      const double slots = (double)kPass3BlocksPerSm * c->num_sms;
       auto eff = [&](double blocks) { const double w = blocks / slots; return w / std::ceil(w); };
       const double tiles = (double)g3.x * g3.y;
       if (eff(2 * tiles) > eff(tiles) + 0.05) {
@@ -783,7 +788,7 @@ int pf_set_tuning(pf_ctx* c, int pairs, int rows1, int rows3) {
            line_smem(c->nx, 3, ty) <= std::max(line_smem(c->nx, 3, 16), (size_t)48 * 1024);
   };
   if (rows1 && (!ok_rows(rows1) || rows1 > 32)) return fail(c, PF_E_ARG, "rows_pass1 %d too large for nx %d", rows1, c->nx);
-  if (rows3 && (!ok_rows(rows3) || (long long)rows3 * c->nx > (long long)kMaxVoxPerThread * kThreadsLine))
+  if (rows3 && (!ok_rows(rows3) || (long long)rows3 * c->nx > max_vox3(c)))
     return fail(c, PF_E_ARG, "rows_pass3 %d too large for nx %d", rows3, c->nx);
   if (rows3 && ((rows3 & (rows3 - 1)) || (c->fast && rows3 < 2)))
     return fail(c, PF_E_ARG, "rows_pass3 must be a power of two (>= 2 for this grid)");
@@ -858,7 +863,7 @@ int pf_autotune(pf_ctx* c, int64_t trial_rotations, int* best_pairs, int* best_r
   }
   for (int r3 : row_cands) {
     if (rc) break;
-    if (r3 == b3 || (long long)r3 * c->nx > (long long)kMaxVoxPerThread * kThreadsLine ||
+    if (r3 == b3 || (long long)r3 * c->nx > max_vox3(c) ||
         line_smem(c->nx, 3, r3) > std::max(line_smem(c->nx, 3, 16), (size_t)48 * 1024))
       continue;
     float ms;

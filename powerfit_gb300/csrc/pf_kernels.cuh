@@ -536,6 +536,16 @@ __device__ __forceinline__ float lcc_value64(float gcc, float ave, float ave2, f
 }
 
 constexpr int kMaxVoxPerThread = 8;   // pass 3: voxels per thread (tile rows * nx <= 8 * 256)
+// fast pass 3: most voxels a tile (rows * nx) may hold
+#ifndef PF_PASS3_MAXVOX
+#define PF_PASS3_MAXVOX 2048
+#endif
+constexpr int kMaxVoxPass3Fast = PF_PASS3_MAXVOX;
+// fast pass 3: resident blocks per SM that its register allocation must allow
+#ifndef PF_PASS3_MINB
+#define PF_PASS3_MINB 2
+#endif
+constexpr int kPass3BlocksPerSm = PF_PASS3_MINB;
 
 #ifdef PF_GENERIC_KERNELS
 __global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {

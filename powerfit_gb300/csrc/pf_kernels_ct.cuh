@@ -431,11 +431,14 @@ __device__ __forceinline__ void pass3_prefetch(const float2* __restrict__ base, 
 #ifndef PF_PASS3_THREADS
 #define PF_PASS3_THREADS 256
 #endif
+#ifndef PF_PASS3_EMAX
+#define PF_PASS3_EMAX 16
+#endif
 constexpr int kThreadsPass3Ct = PF_PASS3_THREADS;
-constexpr int kVoxPass3Ct = (kMaxVoxPerThread * kThreadsLine + kThreadsPass3Ct - 1) / kThreadsPass3Ct;
+constexpr int kVoxPass3Ct = (kMaxVoxPass3Fast + kThreadsPass3Ct - 1) / kThreadsPass3Ct;
 
 template <int X>
-__global__ void __launch_bounds__(kThreadsPass3Ct, 2) k_pass3_ct(const Pass3Params p) {
+__global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct(const Pass3Params p) {
   constexpr int NT = kThreadsPass3Ct, VPT = kVoxPass3Ct;
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
@@ -533,7 +536,7 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, 2) k_pass3_ct(const Pass3Para
     }
     __syncthreads();
     TileLines lines{fld, sh, ty, X * ty};
-    ct_lines<X, true, NT, kEmax>(3 * ty, tw, lines, lines, lines, true, true);
+    ct_lines<X, true, NT, PF_PASS3_EMAX>(3 * ty, tw, lines, lines, lines, true, true);
     const long long ra = p.first_rot + 2LL * pair;
     const bool has_b = ra + 1 < p.nrot;
 #pragma unroll
