@@ -39,6 +39,7 @@ extern "C" {
 #define PF_FLAG_NO_PRUNE 2    /* do not skip rotated rows known to be zero */
 #define PF_FLAG_ACCUMULATE 4  /* keep the running best of earlier scans (do not reset) */
 #define PF_FLAG_GENERIC 8     /* use the runtime-planned kernels even where a specialised path exists */
+#define PF_FLAG_ROT_MAX 16    /* also keep, per rotation, the best LCC over the lcc-mask voxels (pf_get_rotation_max) */
 
 typedef struct pf_ctx pf_ctx;
 
@@ -74,6 +75,16 @@ int pf_set_rotations(pf_ctx *ctx, const double *rotmats, int64_t nrot);
 int pf_reset_results(pf_ctx *ctx);
 int pf_scan_resident(pf_ctx *ctx, int64_t first, int64_t count, int64_t rot_offset, int flags);
 int pf_get_results(pf_ctx *ctx, float *out_lcc, int32_t *out_rot);
+/* After scans with PF_FLAG_ROT_MAX: for rotations first .. first+count-1 of
+ * the uploaded set, the best LCC over the voxels inside the lcc mask (-inf
+ * for a rotation not scanned since its range was last reset).  The per-rotation
+ * score the learned proposal trains on and ranks by; the reference keeps only
+ * the per-voxel best (powerfitter.py:317-333). */
+int pf_get_rotation_max(pf_ctx *ctx, float *out, int64_t first, int64_t count);
+/* The same maxima and, per rotation, the voxel (C-order index) holding it
+ * (-1 where none); either output may be NULL.  Of equal maxima, the higher
+ * voxel index is reported. */
+int pf_get_rotation_best(pf_ctx *ctx, float *value, int32_t *voxel, int64_t first, int64_t count);
 int pf_synchronize(pf_ctx *ctx);
 /* Launch on the caller's cudaStream_t (NULL: back to the context's own
  * non-blocking stream -- so the legacy default stream cannot be selected;
@@ -162,6 +173,26 @@ int pf_laplace_wrap(const double *in, double *out, int nz, int ny, int nx);
 int pf_core_indices(const double *mask, double *out, int nz, int ny, int nx);
 /* message of the last failing preprocessing call */
 int pf_prep_error(char *buf, size_t len);
+
+/* --- learned rotation proposal (device pointers; no reference counterpart) --
+ * The scoring network y = w3 . relu(W2 relu(W1 x + b1) + b2) + b3 with nin
+ * inputs and nh hidden units (16, 32 or 64), bfloat16 weights and float32
+ * accumulation.  Parameters are one flat vector [W1 (nh*nin), b1 (nh),
+ * W2 (nh*nh), b2 (nh), w3 (nh), b3 (1)]: pf_mlp_param_count entries, float32
+ * master copy and bfloat16 copy.  x is row-major (n, nin) float32.  stream:
+ * a cudaStream_t, or NULL for the legacy default stream. */
+int64_t pf_mlp_param_count(int nin, int nh);
+int pf_mlp_forward(const float *x, int64_t n, int nin, int nh, const void *params_bf16, float *y, void *stream);
+/* Adds the gradient of L = sum_i c_i (y_i - t_i)^2, c_i = scale * w_i (w
+ * may be NULL: w_i = 1), into grad (param_count floats) and L into *loss. */
+int pf_mlp_grad(const float *x, const float *t, const float *w, int64_t n, int nin, int nh,
+                const void *params_bf16, float scale, float *grad, float *loss, void *stream);
+/* One Adam step (bias-corrected, step >= 1) on the float32 master
+ * parameters; rewrites the bfloat16 copy. */
+int pf_mlp_adam(float *params, void *params_bf16, const float *grad, float *m, float *v, int64_t count,
+                float lr, float beta1, float beta2, float eps, int step, void *stream);
+/* message of the last failing pf_mlp_* call */
+int pf_mlp_error(char *buf, size_t len);
 
 #ifdef __cplusplus
 }

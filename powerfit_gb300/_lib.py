@@ -18,6 +18,7 @@ PF_FLAG_FP64_NORM = 1
 PF_FLAG_NO_PRUNE = 2
 PF_FLAG_ACCUMULATE = 4
 PF_FLAG_GENERIC = 8
+PF_FLAG_ROT_MAX = 16
 
 EXPORTS = [
     "pf_create", "pf_destroy", "pf_last_error", "pf_global_error", "pf_set_target",
@@ -26,7 +27,8 @@ EXPORTS = [
     "pf_get_geometry", "pf_set_profiling", "pf_get_kernel_times", "pf_fft3d",
     "pf_rotate_grid3d", "pf_conj_multiply", "pf_calc_lcc", "pf_combine",
     "pf_blur_points", "pf_dilate_points", "pf_laplace_wrap", "pf_core_indices", "pf_prep_error",
-    "pf_scan_noalloc",
+    "pf_scan_noalloc", "pf_get_rotation_max", "pf_get_rotation_best",
+    "pf_mlp_param_count", "pf_mlp_forward", "pf_mlp_grad", "pf_mlp_adam", "pf_mlp_error",
 ]
 
 
@@ -99,6 +101,14 @@ def load(path=None):
             "pf_core_indices": (_i, [_vp, _vp, _i, _i, _i]),
             "pf_prep_error": (_i, [ctypes.c_char_p, _sz]),
             "pf_scan_noalloc": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _d, _i, _vp, _i64, _i64, _vp, _vp, _vp]),
+            "pf_get_rotation_max": (_i, [_vp, _vp, _i64, _i64]),
+            "pf_get_rotation_best": (_i, [_vp, _vp, _vp, _i64, _i64]),
+            "pf_mlp_param_count": (_i64, [_i, _i]),
+            "pf_mlp_forward": (_i, [_vp, _i64, _i, _i, _vp, _vp, _vp]),
+            "pf_mlp_grad": (_i, [_vp, _vp, _vp, _i64, _i, _i, _vp, ctypes.c_float, _vp, _vp, _vp]),
+            "pf_mlp_adam": (_i, [_vp, _vp, _vp, _vp, _vp, _i64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                 ctypes.c_float, _i, _vp]),
+            "pf_mlp_error": (_i, [ctypes.c_char_p, _sz]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -145,6 +155,7 @@ class Context:
         self._h = ctypes.c_void_p(h)
         self.shape = (nz, ny, nx)
         self.device = int(device)
+        self.nrot = 0
 
     @property
     def handle(self):
@@ -180,6 +191,7 @@ class Context:
 
     def scan(self, rotmats, rot_offset=0, flags=0):
         r = np.ascontiguousarray(rotmats, dtype=np.float64).reshape(-1, 9)
+        self.nrot = r.shape[0]
         lcc = np.empty(self.shape, dtype=np.float32)
         rot = np.empty(self.shape, dtype=np.int32)
         self._call("pf_scan", ptr(r), r.shape[0], int(rot_offset), ptr(lcc), ptr(rot), int(flags))
@@ -188,6 +200,7 @@ class Context:
     def set_rotations(self, rotmats):
         r = np.ascontiguousarray(rotmats, dtype=np.float64).reshape(-1, 9)
         self._call("pf_set_rotations", ptr(r), r.shape[0])
+        self.nrot = r.shape[0]
         return r.shape[0]
 
     def reset_results(self):
@@ -201,6 +214,23 @@ class Context:
         rot = out_rot if out_rot is not None else np.empty(self.shape, dtype=np.int32)
         self._call("pf_get_results", ptr(lcc), ptr(rot))
         return lcc, rot
+
+    def rotation_max(self, first=0, count=None):
+        """Per-rotation best LCC over the lcc-mask voxels (scans with PF_FLAG_ROT_MAX)."""
+        if count is None:
+            count = self.nrot - first
+        out = np.empty(int(count), dtype=np.float32)
+        self._call("pf_get_rotation_max", ptr(out), int(first), int(count))
+        return out
+
+    def rotation_best(self, first=0, count=None):
+        """(best LCC, voxel index) per rotation (scans with PF_FLAG_ROT_MAX; voxel -1: none)."""
+        if count is None:
+            count = self.nrot - first
+        val = np.empty(int(count), dtype=np.float32)
+        vox = np.empty(int(count), dtype=np.int32)
+        self._call("pf_get_rotation_best", ptr(val), ptr(vox), int(first), int(count))
+        return val, vox
 
     def synchronize(self):
         self._call("pf_synchronize")
@@ -345,3 +375,39 @@ def core_indices(mask):
     out = np.empty_like(m)
     _check_prep(load().pf_core_indices(ptr(m), ptr(out), *m.shape))
     return out
+
+
+# ---- learned proposal: network kernels on device memory --------------------
+
+def check_mlp(rc):
+    if rc != 0:
+        buf = ctypes.create_string_buffer(256)
+        load().pf_mlp_error(buf, 256)
+        raise PowerFitError(rc, buf.value.decode(errors="replace"))
+
+
+def mlp_param_count(nin, nh):
+    return int(load().pf_mlp_param_count(int(nin), int(nh)))
+
+
+def _dp(t):
+    """Device pointer of a CUDA tensor (None -> NULL)."""
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def mlp_forward(x, nin, nh, params_bf16, y, stream=None):
+    """y[i] = net(x[i]) for x (n, nin) float32 on the device (tensors or pointers)."""
+    check_mlp(load().pf_mlp_forward(_dp(x), int(x.shape[0]), int(nin), int(nh), _dp(params_bf16), _dp(y),
+                                    ctypes.c_void_p(stream)))
+
+
+def mlp_grad(x, t, w, nin, nh, params_bf16, scale, grad, loss, stream=None):
+    """grad += dL/dp and loss += L for L = sum_i scale * w_i * (net(x_i) - t_i)^2."""
+    check_mlp(load().pf_mlp_grad(_dp(x), _dp(t), _dp(w), int(x.shape[0]), int(nin), int(nh), _dp(params_bf16),
+                                 float(scale), _dp(grad), _dp(loss), ctypes.c_void_p(stream)))
+
+
+def mlp_adam(params, params_bf16, grad, m, v, lr, step, beta1=0.9, beta2=0.999, eps=1e-8, stream=None):
+    check_mlp(load().pf_mlp_adam(_dp(params), _dp(params_bf16), _dp(grad), _dp(m), _dp(v), int(params.numel()),
+                                 float(lr), float(beta1), float(beta2), float(eps), int(step),
+                                 ctypes.c_void_p(stream)))

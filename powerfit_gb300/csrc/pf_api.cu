@@ -17,6 +17,7 @@
 using namespace pf;
 
 // fast-path kernel tables, one translation unit per cubic grid size
+pf::FastLaunch pf_fast_table_32();
 pf::FastLaunch pf_fast_table_48();
 pf::FastLaunch pf_fast_table_64();
 pf::FastLaunch pf_fast_table_96();
@@ -111,6 +112,8 @@ struct pf_ctx {
   int* rot = nullptr;
   float* part_lcc = nullptr;        // fast pass 3 split over two blocks per tile: best of the later pairs
   int* part_rot = nullptr;
+  unsigned long long* rotmax = nullptr;   // PF_FLAG_ROT_MAX: per-rotation (best LCC, voxel) keys
+  long long rotmax_cap = 0;
   float2* buf = nullptr;
   long long buf_pairs = 0;
   RotFixed* rots = nullptr;
@@ -316,6 +319,7 @@ int set_smem_limits(pf_ctx* c) {
 
 bool fast_table(int n, FastLaunch* fl) {
   switch (n) {
+    case 32: *fl = pf_fast_table_32(); return true;
     case 48: *fl = pf_fast_table_48(); return true;
     case 64: *fl = pf_fast_table_64(); return true;
     case 96: *fl = pf_fast_table_96(); return true;
@@ -528,7 +532,7 @@ int pf_destroy(pf_ctx* c) {
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   c->own_stream = nullptr;
   void* ptrs[] = {c->twx, c->twy, c->twz, c->tmpl, c->mask, c->lcc_mask, c->spec, c->lcc, c->rot, c->buf, c->rots, c->rotd,
-                  c->rows_reach, c->rows_full, c->tmpl_pairs, c->part_lcc, c->part_rot};
+                  c->rows_reach, c->rows_full, c->tmpl_pairs, c->part_lcc, c->part_rot, c->rotmax};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete c;
@@ -659,6 +663,19 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     rc = pf_reset_results(c);
     if (rc) return rc;
   }
+  if (flags & PF_FLAG_ROT_MAX) {
+    if (c->rotmax_cap < c->nrot) {
+      if (c->rotmax) cudaFree(c->rotmax);
+      c->rotmax = nullptr;
+      c->rotmax_cap = 0;
+      rc = alloc(c, (void**)&c->rotmax, std::max<long long>(c->nrot, 1) * sizeof(unsigned long long));
+      if (rc) return rc;
+      c->rotmax_cap = c->nrot;
+      PF_CUDA(c, cudaMemsetAsync(c->rotmax, 0, c->rotmax_cap * sizeof(unsigned long long), c->stream));
+    }
+    if (!(flags & PF_FLAG_ACCUMULATE) && count > 0)
+      PF_CUDA(c, cudaMemsetAsync(c->rotmax + first, 0, count * sizeof(unsigned long long), c->stream));
+  }
   Geometry g = c->g;
   if (flags & PF_FLAG_NO_PRUNE) {
     Geometry full = g;
@@ -720,6 +737,7 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     if (rc) return rc;
     Pass3Params p3{g, c->px, c->twx, c->buf, npairs, r0, end, rot_offset, c->lcc_mask, c->norm_factor,
                    c->lcc, c->rot, ty3, (flags & PF_FLAG_FP64_NORM) ? 1 : 0};
+    if (flags & PF_FLAG_ROT_MAX) p3.rotmax = c->rotmax;
     dim3 g3(c->nz, (c->ny + ty3 - 1) / ty3, 1);
     // Each pass-3 block runs through all pairs of the batch, so a grid of a
     // few waves leaves much of its last wave idle; splitting the pairs over
@@ -761,6 +779,35 @@ int pf_get_results(pf_ctx* c, float* out_lcc, int32_t* out_rot) {
   PF_CUDA(c, cudaStreamSynchronize(c->stream));
   if (c->profiling) collect_events(c);
   return PF_OK;
+}
+
+int pf_get_rotation_best(pf_ctx* c, float* value, int32_t* voxel, int64_t first, int64_t count) {
+  if (!c || (count > 0 && !value && !voxel) || first < 0 || count < 0)
+    return fail(c, PF_E_ARG, "pf_get_rotation_best: bad arguments");
+  if (first + count > c->rotmax_cap) return fail(c, PF_E_STATE, "no per-rotation maxima for that range (scan with PF_FLAG_ROT_MAX)");
+  if (count == 0) return PF_OK;
+  DeviceGuard guard(c->device);
+  std::vector<unsigned long long> keys((size_t)count);
+  PF_CUDA(c, cudaMemcpyAsync(keys.data(), c->rotmax + first, count * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, c->stream));
+  PF_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (int64_t i = 0; i < count; ++i) {
+    const unsigned long long key = keys[(size_t)i];
+    const unsigned int k = (unsigned int)(key >> 32);
+    float f = -INFINITY;
+    if (k) {
+      const unsigned int u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+      std::memcpy(&f, &u, sizeof f);
+    }
+    if (value) value[i] = f;
+    if (voxel) voxel[i] = k ? (int32_t)(unsigned int)(key & 0xffffffffu) : -1;
+  }
+  return PF_OK;
+}
+
+int pf_get_rotation_max(pf_ctx* c, float* out, int64_t first, int64_t count) {
+  if (!c || (!out && count > 0)) return fail(c, PF_E_ARG, "pf_get_rotation_max: bad arguments");
+  return pf_get_rotation_best(c, out, nullptr, first, count);
 }
 
 int pf_synchronize(pf_ctx* c) {

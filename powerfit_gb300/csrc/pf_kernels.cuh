@@ -502,7 +502,56 @@ struct Pass3Params {
   // (merged into lcc / rot afterwards, the earlier half winning ties)
   float* __restrict__ part_lcc = nullptr;
   int* __restrict__ part_rot = nullptr;
+  // with PF_FLAG_ROT_MAX: per rotation of the uploaded set, the best LCC over
+  // the voxels inside the lcc mask and the voxel holding it, as one key:
+  // (order-preserving key of the LCC) << 32 | voxel index (0: none yet)
+  unsigned long long* __restrict__ rotmax = nullptr;
 };
+
+// order-preserving key of a float: a larger float has a larger key, and every
+// float's key is above 0 (which stands for "no value")
+__device__ __forceinline__ unsigned int float_key(float f) {
+  const unsigned int u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// (LCC, voxel) key of one voxel's value; NaN never counts (key 0)
+__device__ __forceinline__ unsigned long long lcc_voxel_key(float v, long long voxel) {
+  return v == v ? ((unsigned long long)float_key(v) << 32) | (unsigned long long)(unsigned int)voxel : 0ull;
+}
+
+// Block-wide max of each thread's keys (ka, kb) -- the best (LCC, voxel) of
+// rotations ra and ra + 1 over the voxels the thread holds -- merged into
+// rotmax[ra], rotmax[ra + 1] by one atomicMax each.  Every thread of the
+// block calls it; `s_red` holds 64 keys; the caller's next barrier makes
+// `s_red` reusable.
+__device__ __forceinline__ void rotmax_block(unsigned long long* rotmax, long long ra, bool has_b,
+                                             unsigned long long ka, unsigned long long kb,
+                                             unsigned long long* s_red) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const unsigned long long oa = __shfl_xor_sync(0xffffffffu, ka, off);
+    const unsigned long long ob = __shfl_xor_sync(0xffffffffu, kb, off);
+    ka = oa > ka ? oa : ka;
+    kb = ob > kb ? ob : kb;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    s_red[warp] = ka;
+    s_red[32 + warp] = kb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    unsigned long long a = 0, b = 0;
+    for (int w = 0; w < nw; ++w) {
+      a = s_red[w] > a ? s_red[w] : a;
+      b = s_red[32 + w] > b ? s_red[32 + w] : b;
+    }
+    if (a) atomicMax(rotmax + ra, a);
+    if (has_b && b) atomicMax(rotmax + ra + 1, b);
+  }
+}
 
 struct GlobalRowsLoad {  // line = f*ty + r, idx = kx: buf[f][kx][z][y0 + r]
   const float2* base;
@@ -550,6 +599,7 @@ constexpr int kPass3BlocksPerSm = PF_PASS3_MINB;
 #ifdef PF_GENERIC_KERNELS
 __global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {
   extern __shared__ float2 sm[];
+  __shared__ unsigned long long s_red[64];
   const Geometry& g = p.g;
   const int X = g.nx;
   float2* tw = sm;
@@ -590,6 +640,7 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {
     __syncthreads();
     const long long ra = p.first_rot + 2LL * pair;
     const bool has_b = ra + 1 < p.nrot;
+    unsigned long long ka = 0, kb = 0;
 #pragma unroll
     for (int k = 0; k < kMaxVoxPerThread; ++k) {
       if (inmask & (1u << k)) {
@@ -608,8 +659,15 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {
         }
         if (la > best[k]) { best[k] = la; brot[k] = (int)(p.rot_offset + ra); }
         if (has_b && lb > best[k]) { best[k] = lb; brot[k] = (int)(p.rot_offset + ra + 1); }
+        if (p.rotmax) {
+          const long long gi = zoff + (long long)(y0 + r) * X + x;
+          const unsigned long long qa = lcc_voxel_key(la, gi), qb = lcc_voxel_key(lb, gi);
+          ka = qa > ka ? qa : ka;
+          kb = qb > kb ? qb : kb;
+        }
       }
     }
+    if (p.rotmax) rotmax_block(p.rotmax, ra, has_b, ka, kb, s_red);
     __syncthreads();
   }
 #pragma unroll

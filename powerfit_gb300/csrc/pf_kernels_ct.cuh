@@ -479,6 +479,7 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct
     }
   }
   __shared__ int s_warp[NT / 32 + 1];
+  __shared__ unsigned long long s_red[64];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int cnt = __popc(inmask);
   int incl = cnt;
@@ -539,6 +540,7 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct
     ct_lines<X, true, NT, PF_PASS3_EMAX>(3 * ty, tw, lines, lines, lines, true, true);
     const long long ra = p.first_rot + 2LL * pair;
     const bool has_b = ra + 1 < p.nrot;
+    unsigned long long ka = 0, kb = 0;
 #pragma unroll
     for (int k = 0; k < VPT; ++k) {
       const int m = threadIdx.x + k * NT;
@@ -559,8 +561,15 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct
         }
         if (la > best[k]) { best[k] = la; brot[k] = (int)(p.rot_offset + ra); }
         if (has_b && lb > best[k]) { best[k] = lb; brot[k] = (int)(p.rot_offset + ra + 1); }
+        if (p.rotmax) {
+          const long long gi = zoff + (long long)(y0 + r) * X + x;
+          const unsigned long long qa = lcc_voxel_key(la, gi), qb = lcc_voxel_key(lb, gi);
+          ka = qa > ka ? qa : ka;
+          kb = qb > kb ? qb : kb;
+        }
       }
     }
+    if (p.rotmax) rotmax_block(p.rotmax, ra, has_b, ka, kb, s_red);
     __syncthreads();
   }
 #pragma unroll

@@ -234,7 +234,7 @@ def test_error_contract(lib):
         ctx.set_tuning(rows1=100000)
 
 
-@pytest.mark.parametrize("n", [48, 64, 96, 128, 160, 192])
+@pytest.mark.parametrize("n", [32, 48, 64, 96, 128, 160, 192])
 def test_fast_path_equals_generic(lib, n):
     """The compile-time-specialised kernels (cubic grids) give the same result
     as the runtime-planned ones."""

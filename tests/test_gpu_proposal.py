@@ -1,0 +1,108 @@
+"""Learned rotation proposal on the GPU: the network's CUDA kernels against
+the float64 oracle (oracle/mlp.py), the per-rotation best LCC against the
+oracle correlator, and the proposal search's exhaustive fallback."""
+import numpy as np
+import pytest
+
+from oracle import mlp
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    torch.cuda.set_device(0)
+    return torch
+
+
+@pytest.mark.parametrize("nin,nh,n", [(15, 32, 1000), (5, 16, 130), (20, 64, 257)])
+def test_network_kernels_match_oracle(torch, nin, nh, n):
+    from powerfit_gb300 import _lib
+    rng = np.random.default_rng(nin * 100 + nh)
+    count = _lib.mlp_param_count(nin, nh)
+    assert count == nh * nin + nh + nh * nh + nh + nh + 1
+    p32 = (rng.normal(size=count) * 0.4).astype(np.float32)
+    pbf = mlp.bf16_round(p32)                       # the values the kernels compute with
+    x = rng.normal(size=(n, nin)).astype(np.float32)
+    t = rng.normal(size=n).astype(np.float32)
+    w = (rng.random(n) + 0.5).astype(np.float32)
+    dev = "cuda:0"
+    pb = torch.tensor(p32, device=dev).to(torch.bfloat16)
+    assert np.array_equal(pb.float().cpu().numpy(), pbf)   # torch's rounding = the oracle's (nearest even)
+    X, T, W = (torch.tensor(a, device=dev) for a in (x, t, w))
+    y = torch.empty(n, device=dev)
+    _lib.mlp_forward(X, nin, nh, pb, y)
+    ref = mlp.forward(pbf, x, nin, nh)
+    assert np.max(np.abs(y.cpu().numpy() - ref)) <= 1e-4 * max(1.0, np.max(np.abs(ref)))
+    for weights in (W, None):
+        grad = torch.zeros(count, device=dev)
+        loss = torch.zeros(1, device=dev)
+        _lib.mlp_grad(X, T, weights, nin, nh, pb, 0.01, grad, loss)
+        L, g = mlp.loss_grad(pbf, x, t, None if weights is None else w, 0.01, nin, nh)
+        assert abs(float(loss.item()) - L) <= 1e-4 * abs(L)
+        err = np.max(np.abs(grad.cpu().numpy() - g))
+        assert err <= 1e-4 * np.max(np.abs(g)), "gradient error %g of max %g" % (err, np.max(np.abs(g)))
+
+
+def test_adam_step_matches_formula(torch):
+    from powerfit_gb300 import _lib
+    rng = np.random.default_rng(7)
+    n = 1601
+    p = rng.normal(size=n).astype(np.float32)
+    g = rng.normal(size=n).astype(np.float32)
+    m = (rng.normal(size=n) * 0.1).astype(np.float32)
+    v = (rng.random(n) * 0.1).astype(np.float32)
+    dev = "cuda:0"
+    P, G, M, V = (torch.tensor(a, device=dev) for a in (p, g, m, v))
+    PB = P.to(torch.bfloat16)
+    lr, b1, b2, eps, step = 1e-3, 0.9, 0.999, 1e-8, 3
+    _lib.mlp_adam(P, PB, G, M, V, lr, step, b1, b2, eps)
+    m1 = b1 * m.astype(np.float64) + (1 - b1) * g
+    v1 = b2 * v.astype(np.float64) + (1 - b2) * g.astype(np.float64) ** 2
+    p1 = p - lr * (m1 / (1 - b1 ** step)) / (np.sqrt(v1 / (1 - b2 ** step)) + eps)
+    assert np.max(np.abs(P.cpu().numpy() - p1)) < 1e-6
+    assert np.array_equal(PB.float().cpu().numpy(), mlp.bf16_round(P.cpu().numpy()))
+
+
+@pytest.mark.parametrize("n,flags", [(32, 0), (24, 0), (32, 8)])
+def test_rotation_max_matches_oracle(n, flags):
+    from powerfit_gb300 import _lib, synth
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    c = synth.make_case((n, n, n), 2.0, 300, 1, 6.0, 4.0, 21)
+    p = O.prepare(c.target.astype(np.float64), c.template, c.mask, False)
+    rot = quat_to_rotmat(super_fibonacci(13))
+    ctx = _lib.Context(p.target.shape)
+    ctx.set_target(p.target, p.lcc_mask)
+    ctx.set_template_mask(p.template, p.mask, float(p.norm_factor), p.rmax)
+    ctx.scan(rot, flags=flags | _lib.PF_FLAG_ROT_MAX)
+    got = ctx.rotation_max()
+    val, vox = ctx.rotation_best()
+    assert np.array_equal(got, val)
+    sel = p.lcc_mask.astype(bool)
+    for i, r in enumerate(rot):
+        lcc = O.lcc_one_rotation(p, r)
+        ref = np.nanmax(lcc[sel])
+        assert abs(got[i] - ref) < 1e-4, (i, got[i], ref)
+        assert sel.ravel()[vox[i]] and abs(lcc.ravel()[vox[i]] - ref) < 1e-4   # the voxel holding it
+    ctx.close()
+
+
+def test_proposal_full_fraction_equals_exhaustive(torch):
+    from powerfit_gb300 import proposal as PR, synth
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    c = synth.make_case((64, 64, 64), 2.0, 1200, 2, 7.0, 4.0, 5)
+    rot = quat_to_rotmat(super_fibonacci(300))
+    pair = PR.SearchPair(c.target, c.template, c.mask, c.voxelspacing, c.resolution, rot)
+    nbr = PR.rotation_neighbours(rot)
+    lcc_x, rot_x = pair.fine_exhaustive()
+    lcc_p, rot_p, sel = PR.proposal_search(pair, None, nbr, fraction=1.0)
+    assert sel.size == rot.shape[0]
+    assert np.array_equal(lcc_p, lcc_x) and np.array_equal(rot_p, rot_x)
+    # a proper subset keeps the set's rotation indices
+    lcc_s, rot_s, sel = PR.proposal_search(pair, None, nbr, fraction=0.2)
+    hit = lcc_s > 0
+    assert np.isin(rot_s[hit], sel).all()
+    assert np.all(lcc_s <= lcc_x + 1e-6)
+    pair.close()
