@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--per-step", type=int, default=0, help="rotations per step (default: set size / 8)")
     ap.add_argument("--cpu-rot-per-core", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--learned-maps", type=int, default=3,
+                    help="held-out 128^3 maps for the learned-proposal leg (0: skip)")
     ap.add_argument("--pairs", type=int, default=0)
     ap.add_argument("--precision", action="store_true",
                     help="precision study: GPU variants vs the float64 oracle on a rotation subset")
@@ -421,8 +423,35 @@ def run_ours(args, rank, world, local_rank):
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": "%d rotations (%d per core) of the same workload, %.1f s, "
                                           "_cpu_scan structure with numpy.fft" % (cn, args.cpu_rot_per_core, cdt)}
+    if args.learned_maps > 0 and world == 1:
+        line["learned"] = learned_leg(args.learned_maps)
     print(json.dumps(line), flush=True)
     return 0
+
+
+def learned_leg(nmaps):
+    """Time to best fit, learned proposal against exhaustive search, on held-out
+    seeded 128^3 maps with the 207,576-rotation set (the trained network shipped
+    in powerfit_gb300/data)."""
+    from powerfit_gb300 import proposal as PR, proposal_train as T
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    rotmats = quat_to_rotmat(super_fibonacci(T.SET_SIZE))
+    nbr = PR.rotation_neighbours(rotmats)
+    net = PR.ProposalNet.load(PR.default_weights())
+    rows = T.evaluate(net, [T.EVAL_SEED0 + i for i in range(nmaps)], 128, rotmats, nbr, log=lambda m: None)
+    summ = T.summarise(rows)
+    return {"metric": "time to best fit, learned proposal vs exhaustive search (128^3, 1 GB300)",
+            "value": summ["network"]["time_vs_exhaustive"], "unit": "fraction of exhaustive time",
+            "higher_is_better": False,
+            "recall": summ["network"]["recall"], "recall_at": summ["network"]["recall_at"],
+            "learned_s": summ["network"]["time_s"], "exhaustive_s": summ["exhaustive_s"],
+            "coarse_only": {"recall": summ["coarse_only"]["recall"], "recall_at": summ["coarse_only"]["recall_at"],
+                            "time_vs_exhaustive": summ["coarse_only"]["time_vs_exhaustive"],
+                            "median_rank_fraction": summ["coarse_only"]["median_rank_fraction"]},
+            "median_rank_fraction": summ["network"]["median_rank_fraction"],
+            "config": {"maps": nmaps, "seeds": "held-out %d.." % T.EVAL_SEED0, "grid": [128, 128, 128],
+                       "rotation_set_size": T.SET_SIZE, "top_fraction": PR.TOP_FRACTION,
+                       "coarse_grid": [PR.COARSE_EDGE] * 3, "data": "synthetic"}}
 
 
 def run_queue(args):

@@ -28,6 +28,7 @@ around the kernels.
 from __future__ import annotations
 
 import math
+import os
 import time
 
 import numpy as np
@@ -246,6 +247,11 @@ def targets(fine_scores, device=0):
     thr = torch.quantile(z, 1.0 - TOP_FRACTION)
     w = 1.0 + 9.0 * (z >= thr).float()
     return z.contiguous(), w.contiguous()
+
+
+def default_weights():
+    """The trained network shipped with the package (see data/proposal_net_report.json)."""
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "proposal_net.npz")
 
 
 class ProposalNet:

@@ -106,3 +106,23 @@ def test_proposal_full_fraction_equals_exhaustive(torch):
     assert np.isin(rot_s[hit], sel).all()
     assert np.all(lcc_s <= lcc_x + 1e-6)
     pair.close()
+
+
+def test_trained_network_ranks_best_fits_higher_than_coarse_score(torch):
+    """What the trained network gains over the method without it: on the
+    validation maps (96^3, the 207,576-rotation set) it ranks the exhaustive
+    best fit higher than the coarse score alone does, and always inside the
+    top 5% that the proposal re-searches."""
+    import math
+    from powerfit_gb300 import proposal as PR, proposal_train as T
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    rot = quat_to_rotmat(super_fibonacci(T.SET_SIZE))
+    nbr = PR.rotation_neighbours(rot)
+    net = PR.ProposalNet.load(PR.default_weights())
+    maps = T.search_data([T.VALID_SEED0 + i for i in range(8)], 96, rot, log=lambda m: None)
+    q_net, _ = T.rank_quality(net, maps, nbr)
+    q_coarse, _ = T.rank_quality(None, maps, nbr)
+    assert q_net < q_coarse - 0.1, (q_net, q_coarse)
+    for m in maps:
+        score = PR.rank_scores(net, m["coarse"], nbr, m["shape"]).float().cpu().numpy()
+        assert T.best_rank(score, m["fine"], T.FOUND_TOL) < math.ceil(PR.TOP_FRACTION * rot.shape[0])
