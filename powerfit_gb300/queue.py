@@ -1,4 +1,5 @@
-"""Queue of maps of uneven size scanned together on one GPU.
+"""Queue of maps of uneven size scanned together on one GPU, on concurrent
+streams or as one captured CUDA graph.
 
 Each map gets its own context (its own compile-time- or runtime-planned
 kernels for its grid) on its own CUDA stream; after the per-map setup
@@ -74,6 +75,71 @@ def scan_queue(jobs, device=0, autotune_trial=256, streams=None):
     for ctx, _ in contexts:
         ctx.close()
     return jobs
+
+
+class QueueGraph:
+    """A queue whose scans are captured once into one CUDA graph.
+
+    Every map keeps its context and stream; the capture forks each map's
+    stream from one capture stream and joins it back, so a replay launches the
+    whole queue -- every map's kernels on its own stream, concurrent as in
+    ``scan_queue`` -- with one graph launch.  Setup (spectra, template,
+    rotations, tuning) and one uncaptured warm-up scan per map, which makes
+    every device buffer, come before the capture.  Each replay recomputes the
+    results from scratch.
+    """
+
+    def __init__(self, jobs, device=0, autotune_trial=256):
+        import torch
+        torch.cuda.set_device(device)
+        self.device = device
+        self.jobs = list(jobs)
+        self.streams = [torch.cuda.Stream(device=device) for _ in self.jobs]
+        self.contexts = []
+        for job, st in zip(self.jobs, self.streams):
+            base = _Prep(job.target, laplace=job.laplace)
+            base.template = job.template
+            base.mask = job.mask
+            ctx = _lib.Context(base._target.shape, device)
+            ctx.set_stream(st.cuda_stream)
+            ftarget = base._laplace_filter(base._target) if job.laplace else base._target
+            ctx.set_target(ftarget, base._lcc_mask)
+            ctx.set_template_mask(base._template, base._mask, float(base._norm_factor), base._rmax)
+            nrot = ctx.set_rotations(job.rotations)
+            if job.pairs:
+                ctx.set_tuning(pairs=job.pairs)
+            elif autotune_trial:
+                ctx.autotune(min(autotune_trial, nrot))
+            self.contexts.append((ctx, nrot))
+        self._scan_all()                        # warm-up: allocates every buffer the scans use
+        torch.cuda.synchronize(device)
+        self.graph = torch.cuda.CUDAGraph()
+        main = torch.cuda.Stream(device=device)
+        with torch.cuda.graph(self.graph, stream=main):
+            for st, (ctx, nrot), job in zip(self.streams, self.contexts, self.jobs):
+                st.wait_stream(main)
+                ctx.scan_resident(0, nrot, job.rot_offset, job.flags)
+                main.wait_stream(st)
+
+    def _scan_all(self):
+        for (ctx, nrot), job in zip(self.contexts, self.jobs):
+            ctx.scan_resident(0, nrot, job.rot_offset, job.flags)
+
+    def replay(self):
+        self.graph.replay()
+
+    def results(self):
+        """Fill every job's ``lcc`` / ``rot`` from the last replay."""
+        import torch
+        torch.cuda.synchronize(self.device)
+        for job, (ctx, _) in zip(self.jobs, self.contexts):
+            job.lcc, job.rot = ctx.get_results()
+        return self.jobs
+
+    def close(self):
+        for ctx, _ in self.contexts:
+            ctx.close()
+        self.contexts = []
 
 
 # The uneven-map workload: 16 seeded maps of 48^3-160^3.

@@ -126,3 +126,22 @@ def test_trained_network_ranks_best_fits_higher_than_coarse_score(torch):
     for m in maps:
         score = PR.rank_scores(net, m["coarse"], nbr, m["shape"]).float().cpu().numpy()
         assert T.best_rank(score, m["fine"], T.FOUND_TOL) < math.ceil(PR.TOP_FRACTION * rot.shape[0])
+
+
+def test_queue_graph_equals_stream_queue(torch):
+    """The uneven-map queue captured into one CUDA graph gives the results of
+    the queue on concurrent streams, replay after replay."""
+    from powerfit_gb300 import synth
+    from powerfit_gb300.queue import MapJob, QueueGraph, scan_queue
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    rot = quat_to_rotmat(super_fibonacci(300))
+    cases = [synth.make_case((n, n, n), 2.0, 600, 1, 7.0, 4.0, 40 + n) for n in (48, 64, 96)]
+    mk = lambda: [MapJob(c.target.astype(np.float64), c.template, c.mask, rot, pairs=16) for c in cases]
+    ref = scan_queue(mk(), autotune_trial=0)
+    qg = QueueGraph(mk(), autotune_trial=0)
+    for _ in range(2):
+        qg.replay()
+        got = qg.results()
+        for a, b in zip(got, ref):
+            assert np.array_equal(a.lcc, b.lcc) and np.array_equal(a.rot, b.rot)
+    qg.close()
