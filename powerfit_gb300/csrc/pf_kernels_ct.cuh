@@ -34,6 +34,51 @@ struct RowListStore {  // line = f*ty + c (row c of the chunk); idx = kx
   }
 };
 
+// periodic index in [0, N) of any offset (a remainder by a compile-time N,
+// no branches); rotations keep offsets within [-N, 2N), but any matrix the
+// library accepts still lands inside the grid
+template <int N>
+__device__ __forceinline__ int wrap_ct(int i) {
+  const int r = i % N;
+  return r < 0 ? r + N : r;
+}
+
+// gather_point_q for an N^3 grid known at compile time: the same values, with
+// 32-bit voxel indices and branch-free wrapping
+template <int N>
+__device__ __forceinline__ void gather_point_ct(const GatherSrc& src, const RotFixed& R, const double* __restrict__ rd,
+                                                const long long* qrow, int cz, int cy, int cx, float& t, float& m) {
+  const long long qx = qrow[0] + R.r[0] * cx;
+  const long long qy = qrow[1] + R.r[1] * cx;
+  const long long qz = qrow[2] + R.r[2] * cx;
+  {
+    const int x0 = (int)(qx >> 32), y0 = (int)(qy >> 32), z0 = (int)(qz >> 32);
+    const float fx = frac_to_float((unsigned int)qx);
+    const float fy = frac_to_float((unsigned int)qy);
+    const float fz = frac_to_float((unsigned int)qz);
+    const int ix0 = wrap_ct<N>(x0);
+    const int iy0 = wrap_ct<N>(y0) * N, iy1 = wrap_ct<N>(y0 + 1) * N;
+    const int iz0 = wrap_ct<N>(z0) * (N * N), iz1 = wrap_ct<N>(z0 + 1) * (N * N);
+    const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
+    const float2* T = src.tmpl_pairs;
+    const float2 a00 = __ldg(T + (iz0 + iy0 + ix0)), a10 = __ldg(T + (iz0 + iy1 + ix0));
+    const float2 a01 = __ldg(T + (iz1 + iy0 + ix0)), a11 = __ldg(T + (iz1 + iy1 + ix0));
+    const float c00 = a00.x * gx + a00.y * fx;
+    const float c10 = a10.x * gx + a10.y * fx;
+    const float c01 = a01.x * gx + a01.y * fx;
+    const float c11 = a11.x * gx + a11.y * fx;
+    const float c0 = c00 * gy + c10 * fy;
+    const float c1 = c01 * gy + c11 * fy;
+    t = c0 * gz + c1 * fz;
+  }
+  {
+    const int x0 = round_fixed(qx, rd, 0, 3, 6, cz, cy, cx);
+    const int y0 = round_fixed(qy, rd, 1, 4, 7, cz, cy, cx);
+    const int z0 = round_fixed(qz, rd, 2, 5, 8, cz, cy, cx);
+    m = __ldg(src.mask + (wrap_ct<N>(z0) * (N * N) + wrap_ct<N>(y0) * N + wrap_ct<N>(x0)));
+  }
+}
+
 // Pass 1 over a list of the (z, y) rows the rotation can reach (built on the
 // host from the template's support): every block transforms `ty` such rows,
 // none is empty and none is outside the reach.
@@ -95,8 +140,8 @@ __global__ void PF_PASS1_BOUNDS k_pass1_ct(const Pass1Params p, const int re2) {
     else { cx = i - (e.z - 1) / 2; x = cx < 0 ? cx + X : cx; }
     const int cz = signed_coord(e.x, g.nz), cy = signed_coord(e.y, g.ny);
     float ta = 0.f, ma = 0.f, tb = 0.f, mb = 0.f;
-    if (has_a) gather_point_q(g, p.src, Ra, rda, s_q[c][0], cz, cy, cx, ta, ma);
-    if (has_b) gather_point_q(g, p.src, Rb, rdb, s_q[c][1], cz, cy, cx, tb, mb);
+    if (has_a) gather_point_ct<X>(p.src, Ra, rda, s_q[c][0], cz, cy, cx, ta, ma);
+    if (has_b) gather_point_ct<X>(p.src, Rb, rdb, s_q[c][1], cz, cy, cx, tb, mb);
     fld[(0 * p.ty + c) * rs + x] = make_float2(ta, -ma);
     fld[(1 * p.ty + c) * rs + x] = make_float2(tb, -mb);
     fld[(2 * p.ty + c) * rs + x] = make_float2(ma * ma, -(mb * mb));
