@@ -20,9 +20,9 @@ proposal path instead
    full-resolution per-rotation best LCC that the exhaustive search generates;
 4. searches the top fraction (5%) of the rotations at full resolution.
 
-The exhaustive search stays the fallback (``fraction=1``) and the judge of the
-proposal: recall is whether the proposal's rotations contain the exhaustive
-best fit.  PyTorch holds the device tensors and does the gathers and top-k
+The exhaustive search stays the fallback (``fraction=1``) and the measure of
+the proposal: recall is whether the proposal's rotations contain the
+exhaustive best fit.  PyTorch holds the device tensors and does the gathers and top-k
 around the kernels.
 """
 from __future__ import annotations
