@@ -75,6 +75,11 @@ int pf_set_rotations(pf_ctx *ctx, const double *rotmats, int64_t nrot);
 int pf_reset_results(pf_ctx *ctx);
 int pf_scan_resident(pf_ctx *ctx, int64_t first, int64_t count, int64_t rot_offset, int flags);
 int pf_get_results(pf_ctx *ctx, float *out_lcc, int32_t *out_rot);
+/* Checkpoint / resume: load a running best saved with pf_get_results (lcc,
+ * rot of nz*ny*nx voxels); a later pf_scan_resident with PF_FLAG_ACCUMULATE
+ * over the remaining rotations continues the search as if never stopped
+ * (the partial maxima merge with _combine semantics, powerfitter.py:146-163). */
+int pf_set_results(pf_ctx *ctx, const float *lcc, const int32_t *rot);
 /* After scans with PF_FLAG_ROT_MAX: for rotations first .. first+count-1 of
  * the uploaded set, the best LCC over the voxels inside the lcc mask (-inf
  * for a rotation not scanned since its range was last reset).  The per-rotation
@@ -193,6 +198,12 @@ int pf_mlp_adam(float *params, void *params_bf16, const float *grad, float *m, f
                 float lr, float beta1, float beta2, float eps, int step, void *stream);
 /* message of the last failing pf_mlp_* call */
 int pf_mlp_error(char *buf, size_t len);
+
+/* --- error-path testing --------------------------------------------------
+ * Make the after-th device allocation of the library from now on (0: the
+ * next) fail as if the device were out of memory, once; -1 turns it off.
+ * The failing call returns PF_E_NOMEM and leaves no partial state behind. */
+int pf_debug_fail_alloc(int64_t after);
 
 #ifdef __cplusplus
 }

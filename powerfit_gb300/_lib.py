@@ -29,6 +29,7 @@ EXPORTS = [
     "pf_blur_points", "pf_dilate_points", "pf_laplace_wrap", "pf_core_indices", "pf_prep_error",
     "pf_scan_noalloc", "pf_get_rotation_max", "pf_get_rotation_best",
     "pf_mlp_param_count", "pf_mlp_forward", "pf_mlp_grad", "pf_mlp_adam", "pf_mlp_error",
+    "pf_set_results", "pf_debug_fail_alloc",
 ]
 
 
@@ -109,6 +110,8 @@ def load(path=None):
             "pf_mlp_adam": (_i, [_vp, _vp, _vp, _vp, _vp, _i64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                  ctypes.c_float, _i, _vp]),
             "pf_mlp_error": (_i, [ctypes.c_char_p, _sz]),
+            "pf_set_results": (_i, [_vp, _vp, _vp]),
+            "pf_debug_fail_alloc": (_i, [_i64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -231,6 +234,14 @@ class Context:
         vox = np.empty(int(count), dtype=np.int32)
         self._call("pf_get_rotation_best", ptr(val), ptr(vox), int(first), int(count))
         return val, vox
+
+    def set_results(self, lcc, rot):
+        """Load a running best (checkpoint) to continue with PF_FLAG_ACCUMULATE."""
+        l = np.ascontiguousarray(lcc, dtype=np.float32)
+        r = np.ascontiguousarray(rot, dtype=np.int32)
+        if l.shape != self.shape or r.shape != self.shape:
+            raise ValueError("checkpoint shape mismatch")
+        self._call("pf_set_results", ptr(l), ptr(r))
 
     def synchronize(self):
         self._call("pf_synchronize")
@@ -411,3 +422,8 @@ def mlp_adam(params, params_bf16, grad, m, v, lr, step, beta1=0.9, beta2=0.999, 
     check_mlp(load().pf_mlp_adam(_dp(params), _dp(params_bf16), _dp(grad), _dp(m), _dp(v), int(params.numel()),
                                  float(lr), float(beta1), float(beta2), float(eps), int(step),
                                  ctypes.c_void_p(stream)))
+
+
+def debug_fail_alloc(after):
+    """Make the `after`-th device allocation from now on fail (-1: off); error-path tests."""
+    check(load().pf_debug_fail_alloc(int(after)))

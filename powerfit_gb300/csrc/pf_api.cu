@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <functional>
 #include <mutex>
 #include <cmath>
@@ -164,7 +165,18 @@ int fail(pf_ctx* c, int code, const char* fmt, ...) {
                                        __FILE__, __LINE__);                                         \
   } while (0)
 
+// Allocation-failure injection (tests of the error paths): the n-th device
+// allocation from now on fails as if the device were out of memory (-1: never).
+std::atomic<long long> g_fail_alloc_after{-1};
+
 int alloc(pf_ctx* c, void** p, size_t bytes) {
+  long long k = g_fail_alloc_after.load();
+  while (k >= 0 && !g_fail_alloc_after.compare_exchange_weak(k, k - 1)) {
+  }
+  if (k == 0) {
+    *p = nullptr;
+    return fail(c, PF_E_NOMEM, "cudaMalloc of %zu bytes failed: injected allocation failure", bytes);
+  }
   cudaError_t e = cudaMalloc(p, bytes);
   if (e != cudaSuccess) {
     *p = nullptr;
@@ -640,6 +652,20 @@ int pf_set_rotations(pf_ctx* c, const double* rotmats, int64_t nrot) {
     PF_CUDA(c, cudaStreamSynchronize(c->stream));
   }
   c->nrot = nrot;
+  return PF_OK;
+}
+
+int pf_set_results(pf_ctx* c, const float* lcc, const int32_t* rot) {
+  if (!c || !lcc || !rot) return fail(c, PF_E_ARG, "pf_set_results: null argument");
+  DeviceGuard guard(c->device);
+  PF_CUDA(c, cudaMemcpyAsync(c->lcc, lcc, c->N * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  PF_CUDA(c, cudaMemcpyAsync(c->rot, rot, c->N * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  PF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PF_OK;
+}
+
+int pf_debug_fail_alloc(int64_t after) {
+  g_fail_alloc_after.store(after < 0 ? -1 : (long long)after);
   return PF_OK;
 }
 

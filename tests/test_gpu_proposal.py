@@ -145,3 +145,40 @@ def test_queue_graph_equals_stream_queue(torch):
         for a, b in zip(got, ref):
             assert np.array_equal(a.lcc, b.lcc) and np.array_equal(a.rot, b.rot)
     qg.close()
+
+
+def test_checkpoint_resume_equals_uninterrupted_scan(tmp_path):
+    """A search stopped after its first chunks and resumed in a new context
+    from the checkpoint gives the uninterrupted search's results."""
+    from powerfit_gb300 import _lib, checkpoint, synth
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    c = synth.make_case((64, 64, 64), 2.0, 900, 2, 7.0, 4.0, 77)
+    p = O.prepare(c.target.astype(np.float64), c.template, c.mask, False)
+    rot = quat_to_rotmat(super_fibonacci(350))
+
+    def context():
+        ctx = _lib.Context(p.target.shape)
+        ctx.set_target(p.target, p.lcc_mask)
+        ctx.set_template_mask(p.template, p.mask, float(p.norm_factor), p.rmax)
+        return ctx
+
+    ref_lcc, ref_rot = context().scan(rot)
+    path = str(tmp_path / "search.npz")
+    lcc, r, done = checkpoint.scan_resumable(context(), rot, path, chunk=100, stop_after=2)
+    assert not done and checkpoint.load(path)[2] == 200
+    lcc, r, done = checkpoint.scan_resumable(context(), rot, path, chunk=100)
+    assert done
+    assert np.array_equal(lcc, ref_lcc) and np.array_equal(r, ref_rot)
+
+
+def test_allocation_failure_is_reported_and_recovered():
+    """An injected device-allocation failure comes back as PF_E_NOMEM with a
+    message, and the next context is unaffected."""
+    from powerfit_gb300 import _lib
+    _lib.debug_fail_alloc(2)
+    with pytest.raises(_lib.PowerFitError) as e:
+        _lib.Context((32, 32, 32))
+    assert e.value.code == -3 and "injected" in str(e.value)
+    _lib.debug_fail_alloc(-1)
+    ctx = _lib.Context((32, 32, 32))
+    ctx.close()
