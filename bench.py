@@ -560,12 +560,81 @@ def _oracle_top2(job):
     return O.scan(p, rots, track_second=True)
 
 
+def run_kernels(args):
+    """One launch of every kernel outside the fast search passes, at 128^3:
+    GPU preprocessing (splat, dilation, Laplace, core weights), the
+    runtime-planned search passes and target spectra (PF_FLAG_GENERIC), the
+    float64 unit mirrors, the shard merge and the proposal network's kernels.
+    Wall time per call (synchronised); meant as the command an ncu capture
+    of these kernels runs."""
+    import torch
+    from powerfit_gb300 import _lib, proposal as PR
+    from powerfit_gb300.correlator import BaseCorrelator
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    torch.cuda.set_device(0)
+    cfg, target, template, mask, rot_all, desc = workload("lcc128_filtered")
+    from powerfit_gb300 import synth
+    case = synth.make_config("lcc128_filtered", seed=0)
+    n = target.shape[0]
+    times = {}
+
+    def timed(name, fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        times[name] = time.perf_counter() - t0
+        return out
+
+    pts = (case.chain / case.voxelspacing).T
+    grid = np.zeros(target.shape)
+    timed("blur_points", lambda: _lib.blur_points(pts, case.elements.astype(np.float64),
+                                                  synth.res_to_sigma(case.resolution) / case.voxelspacing, grid))
+    m = np.zeros(target.shape)
+    timed("dilate_points", lambda: _lib.dilate_points(pts, 5.0 / case.voxelspacing, m))
+    timed("laplace_wrap", lambda: _lib.laplace_wrap(target))
+    timed("core_indices", lambda: _lib.core_indices(m))
+    # runtime-planned search passes and spectra
+    base = BaseCorrelator(target, laplace=True)
+    base.template = template
+    base.mask = mask
+    ctx = _lib.Context(target.shape)
+    timed("set_target (spectra)", lambda: ctx.set_target(_lib.laplace_wrap(base._target), base._lcc_mask))
+    ctx.set_template_mask(base._template, base._mask, float(base._norm_factor), base._rmax)
+    rot = quat_to_rotmat(super_fibonacci(8))
+    timed("scan generic", lambda: ctx.scan(rot, flags=_lib.PF_FLAG_GENERIC))
+    lcc, r = ctx.scan(rot[:2])
+    timed("combine", lambda: _lib.combine_into(lcc.copy(), r.copy(), lcc, r, 0))
+    timed("fft3d", lambda: ctx.fft3d(target.astype(np.float32)))
+    ctx.close()
+    out = np.zeros(target.shape)
+    timed("rotate_grid3d", lambda: _lib.rotate_grid3d(base._template, rot[1], n // 2, out, False))
+    a = np.random.default_rng(0).normal(size=n * n * (n // 2 + 1)) + 0j
+    timed("conj_multiply", lambda: _lib.conj_multiply(a, a, np.empty_like(a)))
+    timed("calc_lcc", lambda: _lib.calc_lcc(target, target, target * target + 1, base._lcc_mask,
+                                            np.empty(target.shape)))
+    # proposal network on the 207,576-rotation set
+    rows = 207576
+    x = torch.randn(rows, PR.FEATURES, device="cuda")
+    t = torch.randn(rows, device="cuda")
+    w = torch.ones(rows, device="cuda")
+    net = PR.ProposalNet.load(PR.default_weights())
+    timed("mlp forward", lambda: net.forward(x))
+    timed("mlp grad", lambda: _lib.mlp_grad(x, t, w, net.nin, net.nh, net.pb, 1.0 / rows, net.grad, net.loss))
+    timed("mlp adam", lambda: _lib.mlp_adam(net.p, net.pb, net.grad, net.m, net.v, 1e-3, 1))
+    print(json.dumps({"metric": "per-call wall time of the auxiliary kernels (128^3)", "unit": "s",
+                      "values": times, "config": {"workload": "kernels", "grid": list(target.shape)}}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.precision:
         return run_precision(args)
     if args.config == "queue16":
         return run_queue(args)
+    if args.config == "kernels":
+        return run_kernels(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
