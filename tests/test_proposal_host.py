@@ -60,3 +60,16 @@ def test_coarse_maps_keep_the_rotation_centre():
     assert np.argmax(ct) == 0                  # fine voxel 0 stays coarse voxel 0
     assert cm[0, 0, 0] == 1 and cm.sum() == 1
     assert PR.coarse_factor(128) == 4 and PR.coarse_factor(48) == 2 and PR.coarse_factor(160) == 5
+
+
+def test_checkpoint_file_round_trip(tmp_path):
+    from powerfit_gb300 import checkpoint
+    rng = np.random.default_rng(3)
+    lcc = rng.random((4, 5, 6)).astype(np.float32)
+    rot = rng.integers(0, 100, size=(4, 5, 6)).astype(np.int32)
+    path = str(tmp_path / "c.npz")
+    checkpoint.save(path, lcc, rot, 40, 100)
+    l2, r2, nxt, nrot = checkpoint.load(path)
+    assert np.array_equal(l2, lcc) and np.array_equal(r2, rot) and (nxt, nrot) == (40, 100)
+    checkpoint.save(path, lcc * 2, rot, 60, 100)          # replaced atomically
+    assert checkpoint.load(path)[2] == 60
