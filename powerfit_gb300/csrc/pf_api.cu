@@ -915,7 +915,7 @@ int pf_autotune(pf_ctx* c, int64_t trial_rotations, int* best_pairs, int* best_r
   size_t freeb = 0, totalb = 0;
   cudaMemGetInfo(&freeb, &totalb);
   const size_t per_pair = 3ull * c->N * sizeof(float2);
-  const int pair_cands[] = {1, 2, 4, 8, 16, 24, 32, 48, 64};
+  const int pair_cands[] = {1, 2, 4, 8, 16, 24, 32, 48, 64, 96, 128};
   for (int pc : pair_cands) {
     if (rc) break;
     if (pc == bp || (size_t)pc * per_pair > (size_t)c->buf_pairs * per_pair + freeb / 2) continue;
