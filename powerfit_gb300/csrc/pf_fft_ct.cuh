@@ -184,40 +184,6 @@ __device__ __forceinline__ void ct_fwd_head(int nlines, const float2* __restrict
   }
 }
 
-// First stage (Ns = 1, no twiddles) of a length-L transform over at most LMAX
-// lines in a single chunk: every item is loaded from `src` and transformed
-// before `bar()` runs, and stored to `dst` after it.  With a cluster-wide
-// barrier this lets a block read other blocks' shared memory and then
-// overwrite its own, which those blocks were reading.
-template <int R, bool INV, int L, int NT, int LMAX, class Src, class Dst, class Bar>
-__device__ __forceinline__ void ct_first_stage_gather(int nlines, const Src& src, const Dst& dst, const Bar& bar) {
-  constexpr int NB = L / R;
-  constexpr int K = (LMAX * NB + NT - 1) / NT;       // items (line, butterfly) per thread
-  float2 v[K][R];
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    const int it = threadIdx.x + k * NT;
-    const int line = it % LMAX;                      // consecutive threads take consecutive lines
-    const int j = it / LMAX;
-    if (j < NB && line < nlines) {
-#pragma unroll
-      for (int r = 0; r < R; ++r) v[k][r] = src.load(line, j + r * NB);
-      DFT<R, INV>::run(v[k]);
-    }
-  }
-  bar();
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    const int it = threadIdx.x + k * NT;
-    const int line = it % LMAX;
-    const int j = it / LMAX;
-    if (j < NB && line < nlines) {
-#pragma unroll
-      for (int r = 0; r < R; ++r) dst.store(line, j * R + r, v[k][r]);
-    }
-  }
-}
-
 // Stages 0 .. nst-2 of a length-L transform, in place in `mid`, each followed
 // by a barrier.
 template <int L, bool INV, int NT, int EMAX, int S, class Mid>

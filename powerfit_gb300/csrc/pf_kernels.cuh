@@ -162,45 +162,6 @@ __device__ __forceinline__ void gather_point(const Geometry& g, const GatherSrc&
   }
 }
 
-// Same values as gather_point, for a point whose row part of q (the cz and cy
-// terms) is precomputed: q = qrow + cx * (r0, r1, r2); the template is read as
-// x-neighbour pairs (one 8-byte load per trilinear edge).
-__device__ __forceinline__ void gather_point_q(const Geometry& g, const GatherSrc& src, const RotFixed& R,
-                                               const double* __restrict__ rd, const long long* qrow, int cz, int cy,
-                                               int cx, float& t, float& m) {
-  SourcePoint s;
-  s.qx = qrow[0] + R.r[0] * cx;
-  s.qy = qrow[1] + R.r[1] * cx;
-  s.qz = qrow[2] + R.r[2] * cx;
-  const long long sxy = (long long)g.nx * g.ny;
-  {
-    const int x0 = (int)(s.qx >> 32), y0 = (int)(s.qy >> 32), z0 = (int)(s.qz >> 32);
-    const float fx = frac_to_float((unsigned int)s.qx);
-    const float fy = frac_to_float((unsigned int)s.qy);
-    const float fz = frac_to_float((unsigned int)s.qz);
-    const int ix0 = wrap1(x0, g.nx);
-    const long long iy0 = (long long)wrap1(y0, g.ny) * g.nx, iy1 = (long long)wrap1(y0 + 1, g.ny) * g.nx;
-    const long long iz0 = (long long)wrap1(z0, g.nz) * sxy, iz1 = (long long)wrap1(z0 + 1, g.nz) * sxy;
-    const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
-    const float2* T = src.tmpl_pairs;
-    const float2 a00 = __ldg(T + iz0 + iy0 + ix0), a10 = __ldg(T + iz0 + iy1 + ix0);
-    const float2 a01 = __ldg(T + iz1 + iy0 + ix0), a11 = __ldg(T + iz1 + iy1 + ix0);
-    const float c00 = a00.x * gx + a00.y * fx;
-    const float c10 = a10.x * gx + a10.y * fx;
-    const float c01 = a01.x * gx + a01.y * fx;
-    const float c11 = a11.x * gx + a11.y * fx;
-    const float c0 = c00 * gy + c10 * fy;
-    const float c1 = c01 * gy + c11 * fy;
-    t = c0 * gz + c1 * fz;
-  }
-  {
-    const int x0 = round_fixed(s.qx, rd, 0, 3, 6, cz, cy, cx);
-    const int y0 = round_fixed(s.qy, rd, 1, 4, 7, cz, cy, cx);
-    const int z0 = round_fixed(s.qz, rd, 2, 5, 8, cz, cy, cx);
-    m = __ldg(src.mask + (long long)wrap1(z0, g.nz) * sxy + (long long)wrap1(y0, g.ny) * g.nx + wrap1(x0, g.nx));
-  }
-}
-
 #ifdef PF_GENERIC_KERNELS
 // tmpl_pairs[i] = (t[i], t[i with x + 1 wrapped])
 __global__ void k_make_pairs(const float* __restrict__ t, float2* __restrict__ out, int nx, long long n) {

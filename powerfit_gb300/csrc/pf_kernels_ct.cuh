@@ -43,8 +43,10 @@ __device__ __forceinline__ int wrap_ct(int i) {
   return r < 0 ? r + N : r;
 }
 
-// gather_point_q for an N^3 grid known at compile time: the same values, with
-// 32-bit voxel indices and branch-free wrapping
+// gather_point for an N^3 grid known at compile time, with the row part of q
+// (the cz and cy terms) precomputed: q = qrow + cx * (r0, r1, r2).  The same
+// values as gather_point, with 32-bit voxel indices, branch-free wrapping and
+// the template read as x-neighbour pairs (one 8-byte load per trilinear edge).
 template <int N>
 __device__ __forceinline__ void gather_point_ct(const GatherSrc& src, const RotFixed& R, const double* __restrict__ rd,
                                                 const long long* qrow, int cz, int cy, int cx, float& t, float& m) {
