@@ -33,6 +33,7 @@ extern "C" {
 #define PF_E_NOMEM (-3)     /* device allocation failed */
 #define PF_E_STATE (-4)     /* target / template / rotations not set */
 #define PF_E_SHAPE (-5)     /* grid size not supported (prime factor > 7, plane too large) */
+#define PF_E_UNSUPPORTED (-6) /* not available in this build of the library */
 
 /* pf_scan flags */
 #define PF_FLAG_FP64_NORM 1   /* local variance and LCC in float64 (default: float-float) */
@@ -204,6 +205,29 @@ int pf_mlp_error(char *buf, size_t len);
  * next) fail as if the device were out of memory, once; -1 turns it off.
  * The failing call returns PF_E_NOMEM and leaves no partial state behind. */
 int pf_debug_fail_alloc(int64_t after);
+
+/* --- bounds-checked build ------------------------------------------------
+ * Built with -DPF_BOUNDS_CHECK (libpowerfit_gb300_checked.so), the search
+ * kernels check every index into global, shared and distributed shared
+ * memory against the extent of its array; an index outside is recorded and
+ * the access skipped (a load reads zero, a store does nothing), never
+ * trapped.  The other build returns PF_E_UNSUPPORTED from these calls.
+ *
+ * 1 when this library was built with bounds checks, else 0. */
+int pf_bounds_checked(void);
+/* Waits for the device, then returns the violations recorded on it since the
+ * last call and clears them: *count violations, *first the code of one of
+ * them ((site << 48) | (index & (2^48 - 1)); 0 when none).  Sites: 1 twiddle
+ * table, 2 shared-memory array, 3 template/mask gather, 4 pass-1 row list,
+ * 5 spectra store, 6 spectra load, 7 target spectrum, 8 output spectra,
+ * 9 cluster push, 10 voxel array, 11 pass-3 voxel list, 12 per-rotation
+ * maximum. */
+int pf_debug_bounds(int device, uint64_t *first, uint64_t *count);
+/* Tell the kernels of this context that the intermediate spectra buffer
+ * holds only `elements` complex values (less than allocated; -1: all), so
+ * that the accesses beyond -- still inside the allocation -- show up as
+ * violations (a test of the checks themselves). */
+int pf_debug_buffer_extent(pf_ctx *ctx, int64_t elements);
 
 #ifdef __cplusplus
 }

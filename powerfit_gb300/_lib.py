@@ -2,6 +2,10 @@
 
 There is no CPU fallback: if the library is missing or cannot be loaded every
 call raises ``NativeLibraryError``.
+
+With ``POWERFIT_GB300_VARIANT=checked`` in the environment the process loads
+``libpowerfit_gb300_checked.so`` instead: the same library built with bounds
+checks in the search kernels (``bounds_checked()``, ``debug_bounds()``).
 """
 from __future__ import annotations
 
@@ -12,7 +16,10 @@ import threading
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libpowerfit_gb300.so")
+VARIANT = os.environ.get("POWERFIT_GB300_VARIANT", "")
+if VARIANT not in ("", "checked"):
+    raise ValueError("POWERFIT_GB300_VARIANT must be empty or 'checked', got %r" % VARIANT)
+LIB_PATH = os.path.join(_HERE, "libpowerfit_gb300_checked.so" if VARIANT == "checked" else "libpowerfit_gb300.so")
 
 PF_FLAG_FP64_NORM = 1
 PF_FLAG_NO_PRUNE = 2
@@ -29,8 +36,15 @@ EXPORTS = [
     "pf_blur_points", "pf_dilate_points", "pf_laplace_wrap", "pf_core_indices", "pf_prep_error",
     "pf_scan_noalloc", "pf_get_rotation_max", "pf_get_rotation_best",
     "pf_mlp_param_count", "pf_mlp_forward", "pf_mlp_grad", "pf_mlp_adam", "pf_mlp_error",
-    "pf_set_results", "pf_debug_fail_alloc",
+    "pf_set_results", "pf_debug_fail_alloc", "pf_bounds_checked", "pf_debug_bounds", "pf_debug_buffer_extent",
 ]
+
+# sites of a bounds-check violation (pf_debug_bounds)
+CHECK_SITES = {
+    1: "twiddle table", 2: "shared-memory array", 3: "template/mask gather", 4: "pass-1 row list",
+    5: "spectra store", 6: "spectra load", 7: "target spectrum", 8: "output spectra", 9: "cluster push",
+    10: "voxel array", 11: "pass-3 voxel list", 12: "per-rotation maximum",
+}
 
 
 class NativeLibraryError(RuntimeError):
@@ -64,8 +78,8 @@ def load(path=None):
         path = path or LIB_PATH
         if not os.path.exists(path):
             raise NativeLibraryError(
-                "libpowerfit_gb300.so not built: run powerfit_gb300.build.build() "
-                "(or __graft_entry__.build()) first; there is no CPU fallback")
+                "%s not built: run powerfit_gb300.build.build() "
+                "(or __graft_entry__.build()) first; there is no CPU fallback" % os.path.basename(path))
         try:
             lib = ctypes.CDLL(path)
         except OSError as e:
@@ -112,6 +126,9 @@ def load(path=None):
             "pf_mlp_error": (_i, [ctypes.c_char_p, _sz]),
             "pf_set_results": (_i, [_vp, _vp, _vp]),
             "pf_debug_fail_alloc": (_i, [_i64]),
+            "pf_bounds_checked": (_i, []),
+            "pf_debug_bounds": (_i, [_i, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
+            "pf_debug_buffer_extent": (_i, [_vp, _i64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -234,6 +251,11 @@ class Context:
         vox = np.empty(int(count), dtype=np.int32)
         self._call("pf_get_rotation_best", ptr(val), ptr(vox), int(first), int(count))
         return val, vox
+
+    def debug_buffer_extent(self, elements):
+        """Bounds-checked build: tell the kernels the intermediate buffer holds
+        only `elements` values (-1: all); accesses beyond count as violations."""
+        self._call("pf_debug_buffer_extent", int(elements))
 
     def set_results(self, lcc, rot):
         """Load a running best (checkpoint) to continue with PF_FLAG_ACCUMULATE."""
@@ -427,3 +449,25 @@ def mlp_adam(params, params_bf16, grad, m, v, lr, step, beta1=0.9, beta2=0.999, 
 def debug_fail_alloc(after):
     """Make the `after`-th device allocation from now on fail (-1: off); error-path tests."""
     check(load().pf_debug_fail_alloc(int(after)))
+
+
+def bounds_checked():
+    """Whether the loaded library is the bounds-checked build."""
+    return bool(load().pf_bounds_checked())
+
+
+def debug_bounds(device=0):
+    """Violations the bounds checks recorded on `device` since the last call
+    (waits for the device; clears them): ``(count, site, index)`` with the
+    site's name and index of one of them (``(0, None, None)`` when none).
+    Raises PowerFitError (PF_E_UNSUPPORTED) on the unchecked build."""
+    first = ctypes.c_uint64(0)
+    count = ctypes.c_uint64(0)
+    check(load().pf_debug_bounds(int(device), ctypes.byref(first), ctypes.byref(count)))
+    if count.value == 0:
+        return 0, None, None
+    code = first.value
+    index = code & ((1 << 48) - 1)
+    if index >= 1 << 47:
+        index -= 1 << 48
+    return int(count.value), CHECK_SITES.get(code >> 48, "site %d" % (code >> 48)), int(index)

@@ -117,6 +117,7 @@ struct pf_ctx {
   long long rotmax_cap = 0;
   float2* buf = nullptr;
   long long buf_pairs = 0;
+  long long debug_buf_extent = -1;   // pf_debug_buffer_extent: extent of buf the kernels are told (-1: all)
   RotFixed* rots = nullptr;
   double* rotd = nullptr;
   int4* rows_reach = nullptr;       // fast pass 1: rows inside the reach disk (pruned)
@@ -168,6 +169,19 @@ int fail(pf_ctx* c, int code, const char* fmt, ...) {
 // Allocation-failure injection (tests of the error paths): the n-th device
 // allocation from now on fails as if the device were out of memory (-1: never).
 std::atomic<long long> g_fail_alloc_after{-1};
+
+#ifdef PF_BOUNDS_CHECK
+// readers of the bounds-check words of every translation unit (pf_check.cuh)
+using CheckTake = int (*)(unsigned long long*, unsigned long long*);
+std::vector<CheckTake>& check_units() {
+  static std::vector<CheckTake> units;
+  return units;
+}
+std::mutex& check_mutex() {
+  static std::mutex m;
+  return m;
+}
+#endif
 
 int alloc(pf_ctx* c, void** p, size_t bytes) {
   long long k = g_fail_alloc_after.load();
@@ -233,6 +247,12 @@ int ensure_part(pf_ctx* c) {
   PF_CUDA(c, cudaMemsetAsync(c->part_lcc, 0, c->N * sizeof(float), c->stream));
   PF_CUDA(c, cudaMemsetAsync(c->part_rot, 0, c->N * sizeof(int), c->stream));
   return PF_OK;
+}
+
+// elements of buf the kernels may address (their bounds checks use it)
+long long buf_extent(const pf_ctx* c) {
+  const long long n = c->buf ? c->buf_pairs * 3 * c->N : 0;
+  return c->debug_buf_extent >= 0 && c->debug_buf_extent < n ? c->debug_buf_extent : n;
 }
 
 int ensure_buf(pf_ctx* c, int pairs) {
@@ -384,16 +404,17 @@ constexpr int kSplitCols = 16;   // columns per tile (step 2b)
 int launch_split_pass2(pf_ctx* c, const Geometry& g, int npairs, int nfield, int mode, float2* out, float scale) {
   const size_t srow = ((size_t)c->ny + (size_t)kSplitRows * (c->ny + kPad)) * sizeof(float2);
   const size_t scol = ((size_t)c->nz + (size_t)c->nz * (kSplitCols + kPad)) * sizeof(float2);
-  SplitRowsParams pr{g, c->py, c->twy, c->buf, nfield, kSplitRows, 0};
+  SplitRowsParams pr{g, c->py, c->twy, c->buf, nfield, kSplitRows, 0, buf_extent(c)};
   dim3 gr((g.nvz + kSplitRows - 1) / kSplitRows, c->nx, npairs * nfield);
   k_split_rows<<<gr, kThreadsLine, srow, c->stream>>>(pr);
   PF_CUDA(c, cudaGetLastError());
-  SplitColsParams pc{g, c->pz, c->twz, c->buf, c->spec, c->spec + c->N, nfield, kSplitCols, mode, out, scale};
+  SplitColsParams pc{g, c->pz, c->twz, c->buf, c->spec, c->spec + c->N, nfield, kSplitCols, mode, out, scale,
+                     buf_extent(c), c->N, out ? 2 * c->N : 0};
   dim3 gc((c->ny + kSplitCols - 1) / kSplitCols, c->nx, npairs * nfield);
   k_split_cols<<<gc, kThreadsLine, scol, c->stream>>>(pc);
   PF_CUDA(c, cudaGetLastError());
   if (mode == 0) {
-    SplitRowsParams pi{g, c->py, c->twy, c->buf, nfield, kSplitRows, 1};
+    SplitRowsParams pi{g, c->py, c->twy, c->buf, nfield, kSplitRows, 1, buf_extent(c)};
     dim3 gi((c->nz + kSplitRows - 1) / kSplitRows, c->nx, npairs * nfield);
     k_split_rows<<<gi, kThreadsLine, srow, c->stream>>>(pi);
     PF_CUDA(c, cudaGetLastError());
@@ -409,7 +430,7 @@ int forward_two_fields(pf_ctx* c, const float* in0, const float* in1, int square
   gfull.nvz = c->nz;
   gfull.zlo = c->nz - 1;
   const int ty = c->ty1;
-  FwdXParams fx{gfull, c->px, c->twx, in0, in1, square1, c->buf, ty};
+  FwdXParams fx{gfull, c->px, c->twx, in0, in1, square1, c->buf, ty, buf_extent(c)};
   dim3 g1(c->nz, (c->ny + ty - 1) / ty, 1);
   k_fwd_x_real<<<g1, kThreadsLine, line_smem(c->nx, 3, ty), c->stream>>>(fx);
   PF_CUDA(c, cudaGetLastError());
@@ -424,6 +445,8 @@ int forward_two_fields(pf_ctx* c, const float* in0, const float* in1, int square
   p2.mode = 1;
   p2.out = out;
   p2.scale = scale;
+  p2.buf_len = buf_extent(c);
+  p2.out_len = 2 * c->N;
   dim3 g2(c->nx, 2, 1);
   if (c->split) {
     int rc2 = launch_split_pass2(c, gfull, 1, 2, 1, out, scale);
@@ -439,6 +462,14 @@ int forward_two_fields(pf_ctx* c, const float* in0, const float* in1, int square
 }
 
 }  // namespace
+
+#ifdef PF_BOUNDS_CHECK
+int pf_check_register(int (*take)(unsigned long long* first, unsigned long long* count)) {
+  std::lock_guard<std::mutex> lock(check_mutex());
+  check_units().push_back(take);
+  return (int)check_units().size();
+}
+#endif
 
 extern "C" {
 
@@ -669,6 +700,48 @@ int pf_debug_fail_alloc(int64_t after) {
   return PF_OK;
 }
 
+int pf_debug_bounds(int device, uint64_t* first, uint64_t* count) {
+#ifdef PF_BOUNDS_CHECK
+  if (!first || !count) return fail(nullptr, PF_E_ARG, "pf_debug_bounds: null output pointer");
+  DeviceGuard guard(device);
+  PF_CUDA(nullptr, cudaDeviceSynchronize());
+  *first = 0;
+  *count = 0;
+  std::lock_guard<std::mutex> lock(check_mutex());
+  for (CheckTake take : check_units()) {
+    unsigned long long f = 0, n = 0;
+    if (take(&f, &n)) return fail(nullptr, PF_E_CUDA, "pf_debug_bounds: cannot read a check word");
+    if (!*first) *first = f;
+    *count += n;
+  }
+  return PF_OK;
+#else
+  (void)device;
+  (void)first;
+  (void)count;
+  return fail(nullptr, PF_E_UNSUPPORTED, "pf_debug_bounds: library built without bounds checks");
+#endif
+}
+
+int pf_debug_buffer_extent(pf_ctx* c, int64_t elements) {
+  if (!c) return PF_E_ARG;
+#ifdef PF_BOUNDS_CHECK
+  c->debug_buf_extent = elements < 0 ? -1 : (long long)elements;
+  return PF_OK;
+#else
+  (void)elements;
+  return fail(c, PF_E_UNSUPPORTED, "pf_debug_buffer_extent: library built without bounds checks");
+#endif
+}
+
+int pf_bounds_checked(void) {
+#ifdef PF_BOUNDS_CHECK
+  return 1;
+#else
+  return 0;
+#endif
+}
+
 int pf_reset_results(pf_ctx* c) {
   if (!c) return PF_E_ARG;
   DeviceGuard guard(c->device);
@@ -722,7 +795,7 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     const int npairs = (int)std::min<int64_t>(P, (end - r0 + 1) / 2);
     const bool full = (flags & PF_FLAG_NO_PRUNE) != 0;
     Pass1Params p1{g, c->px, GatherSrc{c->tmpl, c->mask, c->tmpl_pairs}, c->twx, c->rots, c->rotd, r0, end, c->buf, ty1,
-                   full ? c->rows_full : c->rows_reach, full ? c->nrows_full : c->nrows_reach};
+                   full ? c->rows_full : c->rows_reach, full ? c->nrows_full : c->nrows_reach, buf_extent(c)};
     rc = timed_launch(c, 0, [&] {
       if (fast) {
         if (p1.nrows == 0) return 0;
@@ -747,6 +820,8 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     p2.s2 = c->spec + c->N;
     p2.nfield = 3;
     p2.mode = 0;
+    p2.buf_len = buf_extent(c);
+    p2.spec_len = c->N;
     dim3 g2(c->nx, 3, npairs);
     rc = timed_launch(c, 1, [&] {
       if (fast) {
@@ -763,7 +838,11 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     if (rc) return rc;
     Pass3Params p3{g, c->px, c->twx, c->buf, npairs, r0, end, rot_offset, c->lcc_mask, c->norm_factor,
                    c->lcc, c->rot, ty3, (flags & PF_FLAG_FP64_NORM) ? 1 : 0};
-    if (flags & PF_FLAG_ROT_MAX) p3.rotmax = c->rotmax;
+    if (flags & PF_FLAG_ROT_MAX) {
+      p3.rotmax = c->rotmax;
+      p3.rotmax_len = c->rotmax_cap;
+    }
+    p3.buf_len = buf_extent(c);
     dim3 g3(c->nz, (c->ny + ty3 - 1) / ty3, 1);
     // Each pass-3 block runs through all pairs of the batch, so a grid of a
     // few waves leaves much of its last wave idle; splitting the pairs over
@@ -1167,7 +1246,8 @@ int pf_scan_noalloc(int nz, int ny, int nx, const float* d_target, const uint8_t
     ty1--;
   int ty3 = 16;
   while (ty3 > 1 && (long long)ty3 * nx > (long long)kMaxVoxPerThread * kThreadsLine) ty3 /= 2;
-  FwdXParams fx{g, px, twx, d_target, nullptr, 1, buf, ty1};
+  const long long buf_len = (long long)(kNoAllocBufBytes / sizeof(float2));
+  FwdXParams fx{g, px, twx, d_target, nullptr, 1, buf, ty1, buf_len};
   k_fwd_x_real<<<dim3(nz, (ny + ty1 - 1) / ty1, 1), kThreadsLine, line_smem(nx, 3, ty1), s>>>(fx);
   PF_CUDA(nullptr, cudaGetLastError());
   Pass2Params pt{};
@@ -1181,6 +1261,8 @@ int pf_scan_noalloc(int nz, int ny, int nx, const float* d_target, const uint8_t
   pt.mode = 1;
   pt.out = spec;
   pt.scale = (float)(1.0 / (double)N);
+  pt.buf_len = buf_len;
+  pt.out_len = 2 * N;
   k_pass2<<<dim3(nx, 2, 1), kThreadsPlane, plane_smem(ny, nz), s>>>(pt);
   PF_CUDA(nullptr, cudaGetLastError());
 
@@ -1194,7 +1276,8 @@ int pf_scan_noalloc(int nz, int ny, int nx, const float* d_target, const uint8_t
     k_rot_to_fixed<<<(unsigned)((cn + 127) / 128), 128, 0, s>>>(d_rotmats + 9 * c0, cn, rots);
     PF_CUDA(nullptr, cudaGetLastError());
     for (int64_t r0 = 0; r0 < cn; r0 += 2) {
-      Pass1Params p1{g, px, GatherSrc{d_tmpl, d_mask}, twx, rots, d_rotmats + 9 * c0, r0, cn, buf, ty1, nullptr, 0};
+      Pass1Params p1{g, px, GatherSrc{d_tmpl, d_mask}, twx, rots, d_rotmats + 9 * c0, r0, cn, buf, ty1, nullptr, 0,
+                     buf_len};
       k_pass1<<<dim3(nz, (ny + ty1 - 1) / ty1, 1), kThreadsLine, line_smem(nx, 3, ty1), s>>>(p1);
       Pass2Params p2{};
       p2.g = g;
@@ -1207,9 +1290,12 @@ int pf_scan_noalloc(int nz, int ny, int nx, const float* d_target, const uint8_t
       p2.s2 = spec + N;
       p2.nfield = 3;
       p2.mode = 0;
+      p2.buf_len = buf_len;
+      p2.spec_len = N;
       k_pass2<<<dim3(nx, 3, 1), kThreadsPlane, plane_smem(ny, nz), s>>>(p2);
       Pass3Params p3{g, px, twx, buf, 1, r0, cn, rot_offset + c0, d_lcc_mask, (float)norm_factor,
                      d_lcc, d_rot, ty3, 0};
+      p3.buf_len = buf_len;
       k_pass3<<<dim3(nz, (ny + ty3 - 1) / ty3, 1), kThreadsLine, line_smem(nx, 3, ty3), s>>>(p3);
       PF_CUDA(nullptr, cudaGetLastError());
     }

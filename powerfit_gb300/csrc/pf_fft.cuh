@@ -14,6 +14,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "pf_check.cuh"
+
 namespace pf {
 
 // ---------------------------------------------------------------------------
@@ -262,8 +264,14 @@ struct AxisPlan {
 struct SmemLines {
   float2* base;
   int ls, es;
-  __device__ __forceinline__ float2 load(int line, int idx) const { return base[line * ls + idx * es]; }
-  __device__ __forceinline__ void store(int line, int idx, float2 v) const { base[line * ls + idx * es] = v; }
+  __device__ __forceinline__ float2 load(int line, int idx) const {
+    const float2* q = base + line * ls + idx * es;
+    return PF_CHECK_SMEM(kChkSmem, q, 8) ? *q : make_float2(0.f, 0.f);
+  }
+  __device__ __forceinline__ void store(int line, int idx, float2 v) const {
+    float2* q = base + line * ls + idx * es;
+    if (PF_CHECK_SMEM(kChkSmem, q, 8)) *q = v;
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -295,7 +303,7 @@ __device__ __forceinline__ void fft_stage(int nlines, int L, int Ns, const float
         const int jm = (j % Ns) * twmul;
 #pragma unroll
         for (int r = 1; r < R; ++r) {
-          float2 w = tw[r * jm];
+          float2 w = PF_CHECK(kChkTwiddle, r * jm, L) ? tw[r * jm] : make_float2(1.f, 0.f);
           if (INV) w.y = -w.y;
           v[k][r] = cmul(v[k][r], w);
         }

@@ -112,7 +112,7 @@ __device__ __forceinline__ void ct_stage(int nlines, const float2* __restrict__ 
           const int jm = (j % NS) * TWMUL;
 #pragma unroll
           for (int r = 1; r < R; ++r) {
-            float2 w = tw[r * jm];
+            float2 w = PF_CHECK(kChkTwiddle, r * jm, L) ? tw[r * jm] : make_float2(1.f, 0.f);
             if (INV) w.y = -w.y;
             v[k][r] = cmul(v[k][r], w);
           }
@@ -207,7 +207,7 @@ __device__ __forceinline__ void ct_last_twiddles(const float2* __restrict__ tw, 
   constexpr int NB = L / P.r[P.nst - 1];
   for (int i = threadIdx.x; i < L; i += NT) {
     const int r = i / NB, j = i - r * NB;
-    tl[i] = tw[r * j];
+    if (PF_CHECK(kChkTwiddle, r * j, L) && PF_CHECK_SMEM(kChkSmem, tl + i, 8)) tl[i] = tw[r * j];
   }
 }
 
@@ -231,7 +231,7 @@ __device__ __forceinline__ void ct_last_stage_out(int nlines, const float2* __re
     if constexpr (P.nst > 1) {
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        float2 w = tl[r * NB + j];
+        float2 w = PF_CHECK(kChkTwiddle, r * NB + j, L) ? tl[r * NB + j] : make_float2(1.f, 0.f);
         if (INV) w.y = -w.y;
         v[r] = cmul(v[r], w);
       }
@@ -323,7 +323,8 @@ __device__ __forceinline__ void ct_fwd_mul_inv(int nlines, const float2* __restr
         if constexpr (NB > 1) {           // forward last stage twiddles (Ns = NB)
           const int jm = j;               // (j % NB) * (L / (NB * RL)) with L / (NB * RL) == 1
 #pragma unroll
-          for (int r = 1; r < RL; ++r) v[k][r] = cmul(v[k][r], tw[r * jm]);
+          for (int r = 1; r < RL; ++r)
+            v[k][r] = cmul(v[k][r], PF_CHECK(kChkTwiddle, r * jm, L) ? tw[r * jm] : make_float2(1.f, 0.f));
         }
         DFT<RL, false>::run(v[k]);
 #pragma unroll

@@ -143,6 +143,11 @@ __device__ __forceinline__ void gather_point(const Geometry& g, const GatherSrc&
     const int ix0 = wrap1(x0, g.nx), ix1 = wrap1(x0 + 1, g.nx);
     const long long iy0 = (long long)wrap1(y0, g.ny) * g.nx, iy1 = (long long)wrap1(y0 + 1, g.ny) * g.nx;
     const long long iz0 = (long long)wrap1(z0, g.nz) * sxy, iz1 = (long long)wrap1(z0 + 1, g.nz) * sxy;
+    if (!(PF_CHECK(kChkGather, ix0, g.nx) & PF_CHECK(kChkGather, ix1, g.nx) & PF_CHECK(kChkGather, iy0, sxy) &
+          PF_CHECK(kChkGather, iy1, sxy) & PF_CHECK(kChkGather, iz0, sxy * g.nz) & PF_CHECK(kChkGather, iz1, sxy * g.nz))) {
+      t = m = 0.f;
+      return;
+    }
     const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
     const float* T = src.tmpl;
     const float c00 = __ldg(T + iz0 + iy0 + ix0) * gx + __ldg(T + iz0 + iy0 + ix1) * fx;
@@ -158,7 +163,8 @@ __device__ __forceinline__ void gather_point(const Geometry& g, const GatherSrc&
     const int x0 = round_fixed(s.qx, rd, 0, 3, 6, cz, cy, cx);
     const int y0 = round_fixed(s.qy, rd, 1, 4, 7, cz, cy, cx);
     const int z0 = round_fixed(s.qz, rd, 2, 5, 8, cz, cy, cx);
-    m = __ldg(src.mask + (long long)wrap1(z0, g.nz) * sxy + (long long)wrap1(y0, g.ny) * g.nx + wrap1(x0, g.nx));
+    const long long i = (long long)wrap1(z0, g.nz) * sxy + (long long)wrap1(y0, g.ny) * g.nx + wrap1(x0, g.nx);
+    m = PF_CHECK(kChkGather, i, sxy * g.nz) ? __ldg(src.mask + i) : 0.f;
   }
 }
 
@@ -188,15 +194,18 @@ struct Pass1Params {
   int ty;                               // rows per tile
   const int4* __restrict__ rows;        // fast path: (z, y, points in the sphere, 0) of every reachable row
   int nrows;
+  long long buf_len = 0;                // elements of buf (bounds checks)
 };
 
 struct TransposedStore {  // line = f*ty + r  (row y0 + r of field f); idx = kx
   float2* base;           // buf + pair offset
   int ty, y0, ny, nz, nx, z;
+  long long lim;          // elements from base on (bounds checks)
   __device__ __forceinline__ void store(int line, int idx, float2 v) const {
     const int f = line / ty, r = line - f * ty;
     const int y = y0 + r;
-    if (y < ny) base[(((long long)f * nx + idx) * nz + z) * ny + y] = v;
+    const long long i = (((long long)f * nx + idx) * nz + z) * ny + y;
+    if (y < ny && PF_CHECK(kChkBufStore, i, lim)) base[i] = v;
   }
 };
 
@@ -233,14 +242,17 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass1(const Pass1Params p) {
         if (has_b) gather_point(g, p.src, Rb, rdb, cz, cy, cx, tb, mb);
       }
     }
-    fld[(0 * p.ty + r) * rs + x] = make_float2(ta, -ma);
-    fld[(1 * p.ty + r) * rs + x] = make_float2(tb, -mb);
-    fld[(2 * p.ty + r) * rs + x] = make_float2(ma * ma, -(mb * mb));
+    if (PF_CHECK_SMEM(kChkSmem, fld + (2 * p.ty + r) * rs + x, 8)) {
+      fld[(0 * p.ty + r) * rs + x] = make_float2(ta, -ma);
+      fld[(1 * p.ty + r) * rs + x] = make_float2(tb, -mb);
+      fld[(2 * p.ty + r) * rs + x] = make_float2(ma * ma, -(mb * mb));
+    }
   }
   __syncthreads();
 
   SmemLines lines{fld, rs, 1};
-  TransposedStore out{p.buf + (long long)pair * 3 * g.nx * g.nz * g.ny, p.ty, y0, g.ny, g.nz, g.nx, z};
+  const long long pair_off = (long long)pair * 3 * g.nx * g.nz * g.ny;
+  TransposedStore out{p.buf + pair_off, p.ty, y0, g.ny, g.nz, g.nx, z, p.buf_len - pair_off};
   fft_lines<false, kEmax>(p.px, 3 * p.ty, tw, lines, lines, out, true, false);
 }
 
@@ -261,14 +273,23 @@ struct Pass2Params {
   int mode;                       // 0: correlate (full), 1: forward only -> out
   float2* __restrict__ out;       // mode 1: spectra, layout [f][kx][kz][ky]
   float scale;                    // mode 1: multiply spectra by this
+  long long buf_len = 0;          // elements of buf, of s1 and of s2, of out (bounds checks)
+  long long spec_len = 0;
+  long long out_len = 0;
 };
 
 struct RowMapLines {  // line l -> data row (valid planes only), element idx along y
   float2* base;
   int rs, zlo, shift;
   __device__ __forceinline__ int row(int l) const { return l <= zlo ? l : l + shift; }
-  __device__ __forceinline__ float2 load(int line, int idx) const { return base[row(line) * rs + idx]; }
-  __device__ __forceinline__ void store(int line, int idx, float2 v) const { base[row(line) * rs + idx] = v; }
+  __device__ __forceinline__ float2 load(int line, int idx) const {
+    const float2* q = base + row(line) * rs + idx;
+    return PF_CHECK_SMEM(kChkSmem, q, 8) ? *q : make_float2(0.f, 0.f);
+  }
+  __device__ __forceinline__ void store(int line, int idx, float2 v) const {
+    float2* q = base + row(line) * rs + idx;
+    if (PF_CHECK_SMEM(kChkSmem, q, 8)) *q = v;
+  }
 };
 
 struct ProductStore {  // column transforms: line = ky, idx = kz
@@ -276,8 +297,11 @@ struct ProductStore {  // column transforms: line = ky, idx = kz
   int rs;
   const float2* __restrict__ spec;  // [kz][ky] plane of the target spectrum for this kx
   int ny;
+  long long lim;                    // elements from spec on (bounds checks)
   __device__ __forceinline__ void store(int line, int idx, float2 v) const {
-    base[idx * rs + line] = cmulc(v, __ldg(spec + (long long)idx * ny + line));
+    const long long i = (long long)idx * ny + line;
+    float2* q = base + idx * rs + line;
+    if (PF_CHECK(kChkSpectrum, i, lim) && PF_CHECK_SMEM(kChkSmem, q, 8)) *q = cmulc(v, __ldg(spec + i));
   }
 };
 
@@ -295,14 +319,18 @@ __global__ void __launch_bounds__(kThreadsPlane) k_pass2(const Pass2Params p) {
 
   const int kx = blockIdx.x, f = blockIdx.y, pair = blockIdx.z;
   const long long plane = (long long)Z * Y;
-  float2* gplane = p.buf + (((long long)pair * p.nfield + f) * g.nx + kx) * plane;
+  const long long plane_off = (((long long)pair * p.nfield + f) * g.nx + kx) * plane;
+  float2* gplane = p.buf + plane_off;
+  const long long glim = p.buf_len - plane_off;
 
   // load valid rows, zero the rest
   const int nvz = g.nvz;
   for (int v = threadIdx.x; v < Z * Y; v += blockDim.x) {
     const int z = v / Y, y = v - z * Y;
+    const long long i = (long long)z * Y + y;
     const bool valid = (z <= g.zlo) || (z >= Z - (nvz - g.zlo - 1));
-    pl[z * rs + y] = valid ? gplane[(long long)z * Y + y] : make_float2(0.f, 0.f);
+    if (PF_CHECK_SMEM(kChkSmem, pl + z * rs + y, 8))
+      pl[z * rs + y] = valid && PF_CHECK(kChkBufLoad, i, glim) ? gplane[i] : make_float2(0.f, 0.f);
   }
   __syncthreads();
 
@@ -311,21 +339,25 @@ __global__ void __launch_bounds__(kThreadsPlane) k_pass2(const Pass2Params p) {
   SmemLines cols{pl, 1, rs};
   if (p.mode == 0) {
     const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + (long long)kx * plane;
-    ProductStore prod{pl, rs, spec, Y};
+    ProductStore prod{pl, rs, spec, Y, p.spec_len - (long long)kx * plane};
     fft_lines<false, kEmax>(p.pz, Y, twz, cols, cols, prod, true, true);
     fft_lines<true, kEmax>(p.pz, Y, twz, cols, cols, cols, true, true);
     SmemLines allrows{pl, rs, 1};
     fft_lines<true, kEmax>(p.py, Z, twy, allrows, allrows, allrows, true, true);
     for (int v = threadIdx.x; v < Z * Y; v += blockDim.x) {
       const int z = v / Y, y = v - z * Y;
-      gplane[(long long)z * Y + y] = pl[z * rs + y];
+      const long long i = (long long)z * Y + y;
+      if (PF_CHECK(kChkBufStore, i, glim) && PF_CHECK_SMEM(kChkSmem, pl + z * rs + y, 8)) gplane[i] = pl[z * rs + y];
     }
   } else {
     fft_lines<false, kEmax>(p.pz, Y, twz, cols, cols, cols, true, true);
-    float2* o = p.out + ((long long)f * g.nx + kx) * plane;
+    const long long out_off = ((long long)f * g.nx + kx) * plane;
+    float2* o = p.out + out_off;
     for (int v = threadIdx.x; v < Z * Y; v += blockDim.x) {
       const int z = v / Y, y = v - z * Y;
-      o[(long long)z * Y + y] = cscale(pl[z * rs + y], p.scale);
+      const long long i = (long long)z * Y + y;
+      if (PF_CHECK(kChkOut, i, p.out_len - out_off) && PF_CHECK_SMEM(kChkSmem, pl + z * rs + y, 8))
+        o[i] = cscale(pl[z * rs + y], p.scale);
     }
   }
 }
@@ -348,6 +380,7 @@ struct SplitRowsParams {
   int nfield;
   int rows_per_tile;
   int inverse;     // 0: forward, valid z rows only; 1: inverse, all rows
+  long long buf_len = 0;          // elements of buf (bounds checks)
 };
 
 struct SplitColsParams {
@@ -362,6 +395,9 @@ struct SplitColsParams {
   int mode;                       // 0: z forward, product, z inverse; 1: z forward only -> out
   float2* __restrict__ out;
   float scale;
+  long long buf_len = 0;          // elements of buf, of s1 and of s2, of out (bounds checks)
+  long long spec_len = 0;
+  long long out_len = 0;
 };
 
 #ifdef PF_GENERIC_KERNELS
@@ -379,11 +415,15 @@ __global__ void __launch_bounds__(kThreadsLine) k_split_rows(const SplitRowsPara
   const int nr = min(p.rows_per_tile, nrow_all - r0);
   if (nr <= 0) return;
   const int kx = blockIdx.y;
-  float2* gplane = p.buf + ((long long)blockIdx.z * g.nx + kx) * ((long long)Z * Y);
+  const long long plane_off = ((long long)blockIdx.z * g.nx + kx) * ((long long)Z * Y);
+  float2* gplane = p.buf + plane_off;
+  const long long glim = p.buf_len - plane_off;
   auto row_of = [&](int l) { const int i = r0 + l; return (p.inverse || i <= g.zlo) ? i : i + Z - g.nvz; };
   for (int v = threadIdx.x; v < nr * Y; v += blockDim.x) {
     const int l = v / Y, y = v - l * Y;
-    t[l * rs + y] = gplane[(long long)row_of(l) * Y + y];
+    const long long i = (long long)row_of(l) * Y + y;
+    if (PF_CHECK_SMEM(kChkSmem, t + l * rs + y, 8))
+      t[l * rs + y] = PF_CHECK(kChkBufLoad, i, glim) ? gplane[i] : make_float2(0.f, 0.f);
   }
   __syncthreads();
   SmemLines lines{t, rs, 1};
@@ -391,7 +431,8 @@ __global__ void __launch_bounds__(kThreadsLine) k_split_rows(const SplitRowsPara
   else fft_lines<false, kEmax>(p.py, nr, tw, lines, lines, lines, true, true);
   for (int v = threadIdx.x; v < nr * Y; v += blockDim.x) {
     const int l = v / Y, y = v - l * Y;
-    gplane[(long long)row_of(l) * Y + y] = t[l * rs + y];
+    const long long i = (long long)row_of(l) * Y + y;
+    if (PF_CHECK(kChkBufStore, i, glim) && PF_CHECK_SMEM(kChkSmem, t + l * rs + y, 8)) gplane[i] = t[l * rs + y];
   }
 }
 
@@ -411,30 +452,40 @@ __global__ void __launch_bounds__(kThreadsLine) k_split_cols(const SplitColsPara
   const int pf = blockIdx.z;
   const int f = pf % p.nfield;
   const long long plane = (long long)Z * Y;
-  float2* gplane = p.buf + ((long long)pf * g.nx + kx) * plane;
+  const long long plane_off = ((long long)pf * g.nx + kx) * plane;
+  float2* gplane = p.buf + plane_off;
+  const long long glim = p.buf_len - plane_off;
   const int nvz = g.nvz;
   for (int v = threadIdx.x; v < Z * TC; v += blockDim.x) {
     const int z = v / TC, c = v - z * TC;
+    const long long i = (long long)z * Y + y0 + c;
     const bool valid = c < nc && (p.mode == 1 || z <= g.zlo || z >= Z - (nvz - g.zlo - 1));
-    t[z * rs + c] = valid ? gplane[(long long)z * Y + y0 + c] : make_float2(0.f, 0.f);
+    if (PF_CHECK_SMEM(kChkSmem, t + z * rs + c, 8))
+      t[z * rs + c] = valid && PF_CHECK(kChkBufLoad, i, glim) ? gplane[i] : make_float2(0.f, 0.f);
   }
   __syncthreads();
   SmemLines cols{t, 1, rs};
   if (p.mode == 0) {
-    const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + (long long)kx * plane + y0;
-    ProductStore prod{t, rs, spec, Y};
+    const long long spec_off = (long long)kx * plane + y0;
+    const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + spec_off;
+    ProductStore prod{t, rs, spec, Y, p.spec_len - spec_off};
     fft_lines<false, kEmax>(p.pz, nc, tw, cols, cols, prod, true, true);
     fft_lines<true, kEmax>(p.pz, nc, tw, cols, cols, cols, true, true);
     for (int v = threadIdx.x; v < Z * TC; v += blockDim.x) {
       const int z = v / TC, c = v - z * TC;
-      if (c < nc) gplane[(long long)z * Y + y0 + c] = t[z * rs + c];
+      const long long i = (long long)z * Y + y0 + c;
+      if (c < nc && PF_CHECK(kChkBufStore, i, glim) && PF_CHECK_SMEM(kChkSmem, t + z * rs + c, 8))
+        gplane[i] = t[z * rs + c];
     }
   } else {
     fft_lines<false, kEmax>(p.pz, nc, tw, cols, cols, cols, true, true);
-    float2* o = p.out + ((long long)f * g.nx + kx) * plane;
+    const long long out_off = ((long long)f * g.nx + kx) * plane;
+    float2* o = p.out + out_off;
     for (int v = threadIdx.x; v < Z * TC; v += blockDim.x) {
       const int z = v / TC, c = v - z * TC;
-      if (c < nc) o[(long long)z * Y + y0 + c] = cscale(t[z * rs + c], p.scale);
+      const long long i = (long long)z * Y + y0 + c;
+      if (c < nc && PF_CHECK(kChkOut, i, p.out_len - out_off) && PF_CHECK_SMEM(kChkSmem, t + z * rs + c, 8))
+        o[i] = cscale(t[z * rs + c], p.scale);
     }
   }
 }
@@ -467,6 +518,8 @@ struct Pass3Params {
   // the voxels inside the lcc mask and the voxel holding it, as one key:
   // (order-preserving key of the LCC) << 32 | voxel index (0: none yet)
   unsigned long long* __restrict__ rotmax = nullptr;
+  long long buf_len = 0;       // elements of buf, of rotmax (bounds checks)
+  long long rotmax_len = 0;
 };
 
 // order-preserving key of a float: a larger float has a larger key, and every
@@ -485,8 +538,8 @@ __device__ __forceinline__ unsigned long long lcc_voxel_key(float v, long long v
 // rotations ra and ra + 1 over the voxels the thread holds -- merged into
 // rotmax[ra], rotmax[ra + 1] by one atomicMax each.  Every thread of the
 // block calls it; `s_red` holds 64 keys; the caller's next barrier makes
-// `s_red` reusable.
-__device__ __forceinline__ void rotmax_block(unsigned long long* rotmax, long long ra, bool has_b,
+// `s_red` reusable.  `len`: entries of rotmax (bounds checks).
+__device__ __forceinline__ void rotmax_block(unsigned long long* rotmax, long long len, long long ra, bool has_b,
                                              unsigned long long ka, unsigned long long kb,
                                              unsigned long long* s_red) {
 #pragma unroll
@@ -509,18 +562,20 @@ __device__ __forceinline__ void rotmax_block(unsigned long long* rotmax, long lo
       a = s_red[w] > a ? s_red[w] : a;
       b = s_red[32 + w] > b ? s_red[32 + w] : b;
     }
-    if (a) atomicMax(rotmax + ra, a);
-    if (has_b && b) atomicMax(rotmax + ra + 1, b);
+    if (a && PF_CHECK(kChkRotation, ra, len)) atomicMax(rotmax + ra, a);
+    if (has_b && b && PF_CHECK(kChkRotation, ra + 1, len)) atomicMax(rotmax + ra + 1, b);
   }
 }
 
 struct GlobalRowsLoad {  // line = f*ty + r, idx = kx: buf[f][kx][z][y0 + r]
   const float2* base;
   int ty, y0, ny, nz, nx, z;
+  long long lim;          // elements from base on (bounds checks)
   __device__ __forceinline__ float2 load(int line, int idx) const {
     const int f = line / ty, r = line - f * ty;
     const int y = y0 + r;
-    return y < ny ? base[(((long long)f * nx + idx) * nz + z) * ny + y] : make_float2(0.f, 0.f);
+    const long long i = (((long long)f * nx + idx) * nz + z) * ny + y;
+    return y < ny && PF_CHECK(kChkBufLoad, i, lim) ? base[i] : make_float2(0.f, 0.f);
   }
 };
 
@@ -584,8 +639,8 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {
     if (v < nvox) {
       const int r = v / X, x = v - r * X;
       const int y = y0 + r;
-      if (y < g.ny) {
-        const long long gi = zoff + (long long)y * X + x;
+      const long long gi = zoff + (long long)y * X + x;
+      if (y < g.ny && PF_CHECK(kChkVoxel, gi, (long long)g.nz * g.ny * X)) {
         best[k] = p.lcc[gi];
         brot[k] = p.rot[gi];
         if (p.lcc_mask[gi]) inmask |= 1u << k;
@@ -595,7 +650,8 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {
 
   const long long fstride = (long long)g.nx * g.nz * g.ny;
   for (int pair = 0; pair < p.npairs; ++pair) {
-    GlobalRowsLoad src{p.buf + (long long)pair * 3 * fstride, p.ty, y0, g.ny, g.nz, g.nx, z};
+    GlobalRowsLoad src{p.buf + (long long)pair * 3 * fstride, p.ty, y0, g.ny, g.nz, g.nx, z,
+                       p.buf_len - (long long)pair * 3 * fstride};
     SmemLines lines{fld, rs, 1};
     fft_lines<true, kEmax>(p.px, 3 * p.ty, tw, src, lines, lines, false, true);
     __syncthreads();
@@ -607,9 +663,10 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {
       if (inmask & (1u << k)) {
         const int v = threadIdx.x + k * blockDim.x;
         const int r = v / X, x = v - r * X;
-        const float2 f0 = fld[(0 * p.ty + r) * rs + x];
-        const float2 f1 = fld[(1 * p.ty + r) * rs + x];
-        const float2 f2 = fld[(2 * p.ty + r) * rs + x];
+        const bool in = PF_CHECK_SMEM(kChkSmem, fld + (2 * p.ty + r) * rs + x, 8);
+        const float2 f0 = in ? fld[(0 * p.ty + r) * rs + x] : make_float2(0.f, 0.f);
+        const float2 f1 = in ? fld[(1 * p.ty + r) * rs + x] : make_float2(0.f, 0.f);
+        const float2 f2 = in ? fld[(2 * p.ty + r) * rs + x] : make_float2(0.f, 0.f);
         float la, lb;
         if (p.fp64) {
           la = lcc_value64(f0.x, f0.y, f2.x, p.norm_factor);
@@ -628,7 +685,7 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {
         }
       }
     }
-    if (p.rotmax) rotmax_block(p.rotmax, ra, has_b, ka, kb, s_red);
+    if (p.rotmax) rotmax_block(p.rotmax, p.rotmax_len, ra, has_b, ka, kb, s_red);
     __syncthreads();
   }
 #pragma unroll
@@ -637,8 +694,8 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {
     if (v < nvox) {
       const int r = v / X, x = v - r * X;
       const int y = y0 + r;
-      if (y < g.ny) {
-        const long long gi = zoff + (long long)y * X + x;
+      const long long gi = zoff + (long long)y * X + x;
+      if (y < g.ny && PF_CHECK(kChkVoxel, gi, (long long)g.nz * g.ny * X)) {
         p.lcc[gi] = best[k];
         p.rot[gi] = brot[k];
       }
@@ -660,6 +717,7 @@ struct FwdXParams {
   int square1;                     // field 1 = in0^2 (in1 ignored)
   float2* __restrict__ buf;        // [2][kx][z][y]
   int ty;
+  long long buf_len = 0;           // elements of buf (bounds checks)
 };
 
 #ifdef PF_GENERIC_KERNELS
@@ -677,17 +735,19 @@ __global__ void __launch_bounds__(kThreadsLine) k_fwd_x_real(const FwdXParams p)
     const int r = v / X, x = v - r * X;
     const int y = y0 + r;
     float a = 0.f, b = 0.f;
-    if (y < g.ny) {
-      const long long gi = ((long long)z * g.ny + y) * X + x;
+    const long long gi = ((long long)z * g.ny + y) * X + x;
+    if (y < g.ny && PF_CHECK(kChkVoxel, gi, (long long)g.nz * g.ny * X)) {
       a = p.in0[gi];
       b = p.square1 ? a * a : (p.in1 ? p.in1[gi] : 0.f);
     }
-    fld[r * rs + x] = make_float2(a, 0.f);
-    fld[(p.ty + r) * rs + x] = make_float2(b, 0.f);
+    if (PF_CHECK_SMEM(kChkSmem, fld + (p.ty + r) * rs + x, 8)) {
+      fld[r * rs + x] = make_float2(a, 0.f);
+      fld[(p.ty + r) * rs + x] = make_float2(b, 0.f);
+    }
   }
   __syncthreads();
   SmemLines lines{fld, rs, 1};
-  TransposedStore out{p.buf, p.ty, y0, g.ny, g.nz, g.nx, z};
+  TransposedStore out{p.buf, p.ty, y0, g.ny, g.nz, g.nx, z, p.buf_len};
   fft_lines<false, kEmax>(p.px, 2 * p.ty, tw, lines, lines, out, true, false);
 }
 

@@ -25,11 +25,13 @@ struct RowListStore {  // line = f*ty + c (row c of the chunk); idx = kx
   float2* base;
   const int4* rows;    // shared-memory copy of the chunk's row entries
   int ty, nr, ny, nz;
+  long long lim;       // elements from base on (bounds checks)
   __device__ __forceinline__ void store(int line, int idx, float2 v) const {
     const int f = line / ty, c = line - f * ty;
-    if (c < nr) {
+    if (c < nr && PF_CHECK(kChkRowList, c, 32)) {
       const int4 e = rows[c];
-      base[(((long long)f * X + idx) * nz + e.x) * ny + e.y] = v;
+      const long long i = (((long long)f * X + idx) * nz + e.x) * ny + e.y;
+      if (PF_CHECK(kChkRowList, e.x, nz) & PF_CHECK(kChkRowList, e.y, ny) & PF_CHECK(kChkBufStore, i, lim)) base[i] = v;
     }
   }
 };
@@ -61,6 +63,11 @@ __device__ __forceinline__ void gather_point_ct(const GatherSrc& src, const RotF
     const int ix0 = wrap_ct<N>(x0);
     const int iy0 = wrap_ct<N>(y0) * N, iy1 = wrap_ct<N>(y0 + 1) * N;
     const int iz0 = wrap_ct<N>(z0) * (N * N), iz1 = wrap_ct<N>(z0 + 1) * (N * N);
+    if (!(PF_CHECK(kChkGather, ix0, N) & PF_CHECK(kChkGather, iy0, N * N) & PF_CHECK(kChkGather, iy1, N * N) &
+          PF_CHECK(kChkGather, iz0, N * N * N) & PF_CHECK(kChkGather, iz1, N * N * N))) {
+      t = m = 0.f;
+      return;
+    }
     const float gx = 1.0f - fx, gy = 1.0f - fy, gz = 1.0f - fz;
     const float2* T = src.tmpl_pairs;
     const float2 a00 = __ldg(T + (iz0 + iy0 + ix0)), a10 = __ldg(T + (iz0 + iy1 + ix0));
@@ -77,7 +84,8 @@ __device__ __forceinline__ void gather_point_ct(const GatherSrc& src, const RotF
     const int x0 = round_fixed(qx, rd, 0, 3, 6, cz, cy, cx);
     const int y0 = round_fixed(qy, rd, 1, 4, 7, cz, cy, cx);
     const int z0 = round_fixed(qz, rd, 2, 5, 8, cz, cy, cx);
-    m = __ldg(src.mask + (wrap_ct<N>(z0) * (N * N) + wrap_ct<N>(y0) * N + wrap_ct<N>(x0)));
+    const int i = wrap_ct<N>(z0) * (N * N) + wrap_ct<N>(y0) * N + wrap_ct<N>(x0);
+    m = PF_CHECK(kChkGather, i, N * N * N) ? __ldg(src.mask + i) : 0.f;
   }
 }
 
@@ -93,11 +101,13 @@ __global__ void PF_PASS1_BOUNDS k_pass1_ct(const Pass1Params p, const int re2) {
   float2* fld = sm + X;
   __shared__ int4 s_row[32];
   __shared__ int s_start[33];
+  if (!PF_CHECK(kChkRowList, p.ty - 1, 32)) return;     // tile rows beyond the row arrays (whole block)
   const int c0 = blockIdx.x * p.ty;
   const int nr = min(p.ty, p.nrows - c0);
-  if (threadIdx.x < nr) s_row[threadIdx.x] = p.rows[c0 + threadIdx.x];
+  if (threadIdx.x < nr && PF_CHECK(kChkRowList, c0 + threadIdx.x, p.nrows)) s_row[threadIdx.x] = p.rows[c0 + threadIdx.x];
   for (int i = threadIdx.x; i < X; i += kThreadsLine) tw[i] = p.twx[i];
-  for (int v = threadIdx.x; v < 3 * p.ty * rs; v += kThreadsLine) fld[v] = make_float2(0.f, 0.f);
+  for (int v = threadIdx.x; v < 3 * p.ty * rs; v += kThreadsLine)
+    if (PF_CHECK_SMEM(kChkSmem, fld + v, 8)) fld[v] = make_float2(0.f, 0.f);
   __syncthreads();
   if (threadIdx.x == 0) {
     int acc = 0;
@@ -144,13 +154,16 @@ __global__ void PF_PASS1_BOUNDS k_pass1_ct(const Pass1Params p, const int re2) {
     float ta = 0.f, ma = 0.f, tb = 0.f, mb = 0.f;
     if (has_a) gather_point_ct<X>(p.src, Ra, rda, s_q[c][0], cz, cy, cx, ta, ma);
     if (has_b) gather_point_ct<X>(p.src, Rb, rdb, s_q[c][1], cz, cy, cx, tb, mb);
-    fld[(0 * p.ty + c) * rs + x] = make_float2(ta, -ma);
-    fld[(1 * p.ty + c) * rs + x] = make_float2(tb, -mb);
-    fld[(2 * p.ty + c) * rs + x] = make_float2(ma * ma, -(mb * mb));
+    if (PF_CHECK(kChkRowList, x, X) && PF_CHECK_SMEM(kChkSmem, fld + (2 * p.ty + c) * rs + x, 8)) {
+      fld[(0 * p.ty + c) * rs + x] = make_float2(ta, -ma);
+      fld[(1 * p.ty + c) * rs + x] = make_float2(tb, -mb);
+      fld[(2 * p.ty + c) * rs + x] = make_float2(ma * ma, -(mb * mb));
+    }
   }
   __syncthreads();
   SmemLines lines{fld, rs, 1};
-  RowListStore<X> out{p.buf + (long long)pair * 3 * X * g.nz * g.ny, s_row, p.ty, nr, g.ny, g.nz};
+  const long long pair_off = (long long)pair * 3 * X * g.nz * g.ny;
+  RowListStore<X> out{p.buf + pair_off, s_row, p.ty, nr, g.ny, g.nz, p.buf_len - pair_off};
   ct_lines<X, false, kThreadsLine, kEmax>(3 * p.ty, tw, lines, lines, out, true, false);
 }
 
@@ -166,13 +179,21 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 struct GlobalRows {  // rows of a plane in global memory: line = z, idx = y
   float2* __restrict__ base;
   int ny;
-  __device__ __forceinline__ void store(int line, int idx, float2 v) const { base[(long long)line * ny + idx] = v; }
+  long long lim;      // elements from base on (bounds checks)
+  __device__ __forceinline__ void store(int line, int idx, float2 v) const {
+    const long long i = (long long)line * ny + idx;
+    if (PF_CHECK(kChkBufStore, i, lim)) base[i] = v;
+  }
 };
 
 struct SpectrumOperand {  // target spectrum plane [kz][ky] of this kx
   const float2* __restrict__ spec;
   int ny;
-  __device__ __forceinline__ float2 fetch(int ky, int kz) const { return __ldg(spec + (long long)kz * ny + ky); }
+  long long lim;      // elements from spec on (bounds checks)
+  __device__ __forceinline__ float2 fetch(int ky, int kz) const {
+    const long long i = (long long)kz * ny + ky;
+    return PF_CHECK(kChkSpectrum, i, lim) ? __ldg(spec + i) : make_float2(0.f, 0.f);
+  }
 };
 
 // Block shape of the plane pass: a plane of 128 x 128 or more fills one block
@@ -199,7 +220,9 @@ __global__ void __launch_bounds__(PlaneLaunch<Y, Z>::kThreads, PlaneLaunch<Y, Z>
 
   const int kx = blockIdx.x, f = blockIdx.y, pair = blockIdx.z;
   constexpr long long plane = (long long)Z * Y;
-  float2* gplane = p.buf + (((long long)pair * p.nfield + f) * g.nx + kx) * plane;
+  const long long plane_off = (((long long)pair * p.nfield + f) * g.nx + kx) * plane;
+  float2* gplane = p.buf + plane_off;
+  const long long glim = p.buf_len - plane_off;
   const int nvz = g.nvz;
   const int lo_end = g.zlo, hi_start = Z - (nvz - g.zlo - 1);
 
@@ -209,7 +232,8 @@ __global__ void __launch_bounds__(PlaneLaunch<Y, Z>::kThreads, PlaneLaunch<Y, Z>
     const int z = v / Y, y = v - z * Y;
     const bool valid = p.mode != 0 ||
                        ((z <= lo_end || z >= hi_start) && row_in_disk(g, signed_coord(z, Z), signed_coord(y, Y), re2));
-    if (valid) cp_async8(pl + z * rs + y, gplane + (long long)z * Y + y);
+    if (!PF_CHECK_SMEM(kChkSmem, pl + z * rs + y, 8)) continue;
+    if (valid && PF_CHECK(kChkBufLoad, (long long)z * Y + y, glim)) cp_async8(pl + z * rs + y, gplane + (long long)z * Y + y);
     else pl[z * rs + y] = make_float2(0.f, 0.f);
   }
   for (int i = threadIdx.x; i < Y; i += kThreadsPlaneCt) twy[i] = p.twy[i];
@@ -223,17 +247,20 @@ __global__ void __launch_bounds__(PlaneLaunch<Y, Z>::kThreads, PlaneLaunch<Y, Z>
   SmemLines cols{pl, 1, rs};
   if (p.mode == 0) {
     const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + (long long)kx * plane;
-    ct_fwd_mul_inv<Z, kThreadsPlaneCt, kEmax>(Y, twz, cols, SpectrumOperand{spec, Y}, cols, true);
+    ct_fwd_mul_inv<Z, kThreadsPlaneCt, kEmax>(Y, twz, cols, SpectrumOperand{spec, Y, p.spec_len - (long long)kx * plane},
+                                              cols, true);
     // inverse y: all stages but the last in place, the last one straight to the buffer
     SmemLines allrows{pl, rs, 1};
     ct_head_inplace<Y, true, kThreadsPlaneCt, kEmax, 0>(Z, twy, allrows);
-    ct_last_stage_out<Y, true, kThreadsPlaneCt>(Z, tly, allrows, GlobalRows{gplane, Y});
+    ct_last_stage_out<Y, true, kThreadsPlaneCt>(Z, tly, allrows, GlobalRows{gplane, Y, glim});
   } else {
     ct_lines<Z, false, kThreadsPlaneCt, kEmax>(Y, twz, cols, cols, cols, true, true);
-    float2* o = p.out + ((long long)f * g.nx + kx) * plane;
+    const long long out_off = ((long long)f * g.nx + kx) * plane;
+    float2* o = p.out + out_off;
     for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlaneCt) {
       const int z = v / Y, y = v - z * Y;
-      o[(long long)z * Y + y] = cscale(pl[z * rs + y], p.scale);
+      if (PF_CHECK(kChkOut, (long long)z * Y + y, p.out_len - out_off) && PF_CHECK_SMEM(kChkSmem, pl + z * rs + y, 8))
+        o[(long long)z * Y + y] = cscale(pl[z * rs + y], p.scale);
     }
   }
 }
@@ -294,7 +321,9 @@ struct PushToColumns {  // A's last stage: line = own valid row, idx = ky -> col
     const int i = i0 + line;
     const int z = i <= zlo ? i : i + shift;
     const int owner = ky / CW;
-    st_cluster(cols.get(owner) + (unsigned int)((z * (CW + kPad) + ky - owner * CW) * sizeof(float2)), v);
+    const int off = z * (CW + kPad) + ky - owner * CW;    // column array [Z][CW + kPad] of the owner
+    if (PF_CHECK(kChkCluster, owner, CS) & PF_CHECK(kChkCluster, off, Z * (CW + kPad)))
+      st_cluster(cols.get(owner) + (unsigned int)(off * sizeof(float2)), v);
   }
 };
 
@@ -303,9 +332,12 @@ struct PushToRows {  // B's last stage: line = own column (ky - ky0), idx = z ->
   static constexpr int ZB = Z / CS;
   ClusterBases<CS> rows;
   int ky0;
+  int cap;             // elements of a block's row array (bounds checks)
   __device__ __forceinline__ void store(int line, int z, float2 v) const {
     const int owner = z / ZB;
-    st_cluster(rows.get(owner) + (unsigned int)(((z - owner * ZB) * (Y + kPad) + ky0 + line) * sizeof(float2)), v);
+    const int off = (z - owner * ZB) * (Y + kPad) + ky0 + line;
+    if (PF_CHECK(kChkCluster, owner, CS) & PF_CHECK(kChkCluster, off, cap))
+      st_cluster(rows.get(owner) + (unsigned int)(off * sizeof(float2)), v);
   }
 };
 
@@ -347,7 +379,9 @@ __global__ void __launch_bounds__(ClusterPlane<Y, Z, CS>::kThreads, ClusterPlane
 
   const int kx = blockIdx.y, f = blockIdx.z % p.nfield, pair = blockIdx.z / p.nfield;
   constexpr long long plane = (long long)Z * Y;
-  float2* gplane = p.buf + (((long long)pair * p.nfield + f) * g.nx + kx) * plane;
+  const long long plane_off = (((long long)pair * p.nfield + f) * g.nx + kx) * plane;
+  float2* gplane = p.buf + plane_off;
+  const long long glim = p.buf_len - plane_off;
 
   // A. own valid rows: the entries the rotation can reach, zeros elsewhere;
   // zeros in the column array's rows outside the valid planes (no block pushes those)
@@ -357,14 +391,16 @@ __global__ void __launch_bounds__(ClusterPlane<Y, Z, CS>::kThreads, ClusterPlane
     const int li = v / Y, y = v - li * Y;
     const int i = i0 + li;
     const int z = i <= zlo ? i : i + shift;
-    if (row_in_disk(g, signed_coord(z, Z), signed_coord(y, Y), re2))
+    if (!PF_CHECK_SMEM(kChkSmem, rows + li * (Y + kPad) + y, 8)) continue;
+    if (row_in_disk(g, signed_coord(z, Z), signed_coord(y, Y), re2) && PF_CHECK(kChkBufLoad, (long long)z * Y + y, glim))
       cp_async8(rows + li * (Y + kPad) + y, gplane + (long long)z * Y + y);
     else
       rows[li * (Y + kPad) + y] = make_float2(0.f, 0.f);
   }
   for (int v = threadIdx.x; v < (hi_start - zlo - 1) * CW; v += NT) {
     const int zi = v / CW, col = v - zi * CW;
-    cols[(zlo + 1 + zi) * (CW + kPad) + col] = make_float2(0.f, 0.f);
+    if (PF_CHECK(kChkSmem, (zlo + 1 + zi) * (CW + kPad) + col, Z * (CW + kPad)))
+      cols[(zlo + 1 + zi) * (CW + kPad) + col] = make_float2(0.f, 0.f);
   }
   for (int i = threadIdx.x; i < Y; i += NT) twy[i] = p.twy[i];
   for (int i = threadIdx.x; i < Z; i += NT) twz[i] = p.twz[i];
@@ -386,16 +422,19 @@ __global__ void __launch_bounds__(ClusterPlane<Y, Z, CS>::kThreads, ClusterPlane
 
   // B. own columns: z transform, product, inverse z; the last stage pushes rows
   SmemLines own_cols{cols, 1, CW + kPad};
-  const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + (long long)kx * plane + c * CW;
-  PushToRows<Y, Z, CS> to_rows{brows, c * CW};
-  ct_fwd_mul_inv<Z, NT, kEmax>(CW, twz, own_cols, SpectrumOperand{spec, Y}, own_cols, true, &to_rows);
+  const long long spec_off = (long long)kx * plane + c * CW;
+  const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + spec_off;
+  PushToRows<Y, Z, CS> to_rows{brows, c * CW, max(rb, ZB) * (Y + kPad)};
+  ct_fwd_mul_inv<Z, NT, kEmax>(CW, twz, own_cols, SpectrumOperand{spec, Y, p.spec_len - spec_off}, own_cols, true,
+                               &to_rows);
   cluster_arrive();
   cluster_wait();                          // every row array is complete; no more remote stores
 
   // C. own z rows: inverse y, the last stage straight to the buffer
   SmemLines out_rows{rows, Y + kPad, 1};
   ct_head_inplace<Y, true, NT, kEmax, 0>(ZB, twy, out_rows);
-  ct_last_stage_out<Y, true, NT>(ZB, tly, out_rows, GlobalRows{gplane + (long long)c * ZB * Y, Y});
+  ct_last_stage_out<Y, true, NT>(ZB, tly, out_rows, GlobalRows{gplane + (long long)c * ZB * Y, Y,
+                                                                glim - (long long)c * ZB * Y});
 }
 
 // Whether one block holds a whole N x N plane (twiddles, plane, last-stage
@@ -447,14 +486,21 @@ struct TileLines {
   float2* base;
   int sh, ty, xty;      // log2(ty), ty, X*ty
   __device__ __forceinline__ int off(int line) const { return (line >> sh) * xty + (line & (ty - 1)); }
-  __device__ __forceinline__ float2 load(int line, int idx) const { return base[off(line) + idx * ty]; }
-  __device__ __forceinline__ void store(int line, int idx, float2 v) const { base[off(line) + idx * ty] = v; }
+  __device__ __forceinline__ float2 load(int line, int idx) const {
+    const float2* q = base + off(line) + idx * ty;
+    return PF_CHECK_SMEM(kChkSmem, q, 8) ? *q : make_float2(0.f, 0.f);
+  }
+  __device__ __forceinline__ void store(int line, int idx, float2 v) const {
+    float2* q = base + off(line) + idx * ty;
+    if (PF_CHECK_SMEM(kChkSmem, q, 8)) *q = v;
+  }
 };
 
 template <int X, int NT>
-__device__ __forceinline__ void pass3_prefetch(const float2* __restrict__ base, float2* fld, int ty, int y0, int ny,
-                                               int nz, int z) {
-  // buf[f][kx][z][y0 .. y0+ty) -> fld[(f*X + kx)*ty .. +ty): 16-byte copies (two rows each)
+__device__ __forceinline__ void pass3_prefetch(const float2* __restrict__ base, long long lim, float2* fld, int ty,
+                                               int y0, int ny, int nz, int z) {
+  // buf[f][kx][z][y0 .. y0+ty) -> fld[(f*X + kx)*ty .. +ty): 16-byte copies (two rows each);
+  // `lim`: elements from base on (bounds checks)
   const int halfty = ty >> 1;
   const int n = 3 * X * halfty;
   const int sh = __ffs(halfty) - 1;
@@ -462,12 +508,16 @@ __device__ __forceinline__ void pass3_prefetch(const float2* __restrict__ base, 
   if (y0 + ty <= ny) {
     for (int v = threadIdx.x; v < n; v += NT) {
       const int fk = v >> sh, part = v & (halfty - 1);
-      cp_async16(fld + fk * ty + 2 * part, base + (long long)fk * nz * ny + zrow + 2 * part);
+      const long long i = (long long)fk * nz * ny + zrow + 2 * part;
+      if (PF_CHECK(kChkBufLoad, i + 1, lim) && PF_CHECK_SMEM(kChkSmem, fld + fk * ty + 2 * part, 16))
+        cp_async16(fld + fk * ty + 2 * part, base + i);
     }
   } else {   // last tile of an edge not divisible by ty
     for (int v = threadIdx.x; v < 3 * X * ty; v += NT) {
       const int fk = v / ty, r = v - fk * ty;
-      if (y0 + r < ny) cp_async8(fld + fk * ty + r, base + (long long)fk * nz * ny + zrow + r);
+      const long long i = (long long)fk * nz * ny + zrow + r;
+      if (!PF_CHECK_SMEM(kChkSmem, fld + fk * ty + r, 8)) continue;
+      if (y0 + r < ny && PF_CHECK(kChkBufLoad, i, lim)) cp_async8(fld + fk * ty + r, base + i);
       else fld[fk * ty + r] = make_float2(0.f, 0.f);
     }
   }
@@ -508,7 +558,9 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct
   const int pe = gridDim.z == 1 ? p.npairs : (blockIdx.z == 0 ? half : p.npairs);
 
   // start the first tile's copies before anything else
-  if (pb < pe) pass3_prefetch<X, NT>(p.buf + (long long)pb * 3 * fstride, fbuf0, ty, y0, g.ny, g.nz, z);
+  if (pb < pe)
+    pass3_prefetch<X, NT>(p.buf + (long long)pb * 3 * fstride, p.buf_len - (long long)pb * 3 * fstride, fbuf0, ty, y0,
+                          g.ny, g.nz, z);
   cp_async_commit();
   for (int i = threadIdx.x; i < X; i += NT) tw[i] = p.twx[i];
 
@@ -522,7 +574,8 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct
     const int v = threadIdx.x + k * NT;
     if (v < nvox) {
       const int y = y0 + (v & (ty - 1));
-      if (y < g.ny && p.lcc_mask[zoff + (long long)y * X + (v >> sh)]) inmask |= 1u << k;
+      const long long gi = zoff + (long long)y * X + (v >> sh);
+      if (y < g.ny && PF_CHECK(kChkVoxel, gi, (long long)g.nz * g.ny * X) && p.lcc_mask[gi]) inmask |= 1u << k;
     }
   }
   __shared__ int s_warp[NT / 32 + 1];
@@ -551,7 +604,10 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct
     int pos = s_warp[warp] + incl - cnt;
 #pragma unroll
     for (int k = 0; k < VPT; ++k)
-      if (inmask & (1u << k)) s_list[pos++] = (unsigned short)(threadIdx.x + k * NT);
+      if (inmask & (1u << k)) {
+        if (PF_CHECK(kChkVoxelList, pos, 4 * pass3_list_slots(X, ty))) s_list[pos] = (unsigned short)(threadIdx.x + k * NT);
+        ++pos;
+      }
   }
   __syncthreads();
   const int total = s_warp[NT / 32];
@@ -564,19 +620,21 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct
     const int m = threadIdx.x + k * NT;
     best[k] = 0.f;
     brot[k] = 0;
-    if (m < total && blockIdx.z == 0) {
+    if (m < total && blockIdx.z == 0 && PF_CHECK(kChkVoxelList, m, 4 * pass3_list_slots(X, ty))) {
       const int v = s_list[m];
       const long long gi = zoff + (long long)(y0 + (v & (ty - 1))) * X + (v >> sh);
-      best[k] = p.lcc[gi];
-      brot[k] = p.rot[gi];
+      if (PF_CHECK(kChkVoxel, gi, (long long)g.nz * g.ny * X)) {
+        best[k] = p.lcc[gi];
+        brot[k] = p.rot[gi];
+      }
     }
   }
 
   for (int pair = pb; pair < pe; ++pair) {
     float2* fld = fbuf0 + ((pair - pb) & 1) * fbuf_stride;
     if (pair + 1 < pe) {
-      pass3_prefetch<X, NT>(p.buf + (long long)(pair + 1) * 3 * fstride, fbuf0 + ((pair + 1 - pb) & 1) * fbuf_stride,
-                            ty, y0, g.ny, g.nz, z);
+      pass3_prefetch<X, NT>(p.buf + (long long)(pair + 1) * 3 * fstride, p.buf_len - (long long)(pair + 1) * 3 * fstride,
+                            fbuf0 + ((pair + 1 - pb) & 1) * fbuf_stride, ty, y0, g.ny, g.nz, z);
       cp_async_commit();
       cp_async_wait_group<1>();
     } else {
@@ -591,13 +649,14 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct
 #pragma unroll
     for (int k = 0; k < VPT; ++k) {
       const int m = threadIdx.x + k * NT;
-      if (m < total) {
+      if (m < total && PF_CHECK(kChkVoxelList, m, 4 * pass3_list_slots(X, ty))) {
         const int v = s_list[m];
         const int r = v & (ty - 1), x = v >> sh;
         const int o = x * ty + r;
-        const float2 f0 = fld[o];
-        const float2 f1 = fld[X * ty + o];
-        const float2 f2 = fld[2 * X * ty + o];
+        const bool in = PF_CHECK(kChkVoxelList, v, nvox) && PF_CHECK_SMEM(kChkSmem, fld + 2 * X * ty + o, 8);
+        const float2 f0 = in ? fld[o] : make_float2(0.f, 0.f);
+        const float2 f1 = in ? fld[X * ty + o] : make_float2(0.f, 0.f);
+        const float2 f2 = in ? fld[2 * X * ty + o] : make_float2(0.f, 0.f);
         float la, lb;
         if (p.fp64) {
           la = lcc_value64(f0.x, f0.y, f2.x, p.norm_factor);
@@ -616,17 +675,19 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct
         }
       }
     }
-    if (p.rotmax) rotmax_block(p.rotmax, ra, has_b, ka, kb, s_red);
+    if (p.rotmax) rotmax_block(p.rotmax, p.rotmax_len, ra, has_b, ka, kb, s_red);
     __syncthreads();
   }
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
     const int m = threadIdx.x + k * NT;
-    if (m < total) {
+    if (m < total && PF_CHECK(kChkVoxelList, m, 4 * pass3_list_slots(X, ty))) {
       const int v = s_list[m];
       const long long gi = zoff + (long long)(y0 + (v & (ty - 1))) * X + (v >> sh);
-      out_lcc[gi] = best[k];
-      out_rot[gi] = brot[k];
+      if (PF_CHECK(kChkVoxel, gi, (long long)g.nz * g.ny * X)) {
+        out_lcc[gi] = best[k];
+        out_rot[gi] = brot[k];
+      }
     }
   }
 }

@@ -1,0 +1,86 @@
+"""The bounds-checked build on the GPU.
+
+The search kernels built with -DPF_BOUNDS_CHECK check every index into
+global, shared and distributed shared memory against its array's extent and
+record (never trap on) a violation.  tests/bounds_cases.py runs the scans of
+every kernel family through that build in a child process (the variant is
+chosen when the library loads); this test then asks:
+
+* no case recorded a violation;
+* the checks see accesses beyond a shrunk buffer extent (the accesses stay
+  inside the allocation, so the shrunk runs are safe), and a run with the
+  extent restored is clean and gives the first run's results;
+* the checked build's results are the unchecked build's (the checks change
+  no arithmetic) -- and on the tiny and odd grids the oracle's, by the parity
+  criterion of the other GPU tests (best LCC within 1e-4; best rotation equal
+  where the top-two gap exceeds 1e-4).
+"""
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+import bounds_cases as B
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def checked_run(tmp_path_factory):
+    from powerfit_gb300 import build
+    build.build(variant="checked")
+    out = str(tmp_path_factory.mktemp("bounds") / "checked.npz")
+    env = dict(os.environ, POWERFIT_GB300_VARIANT="checked")
+    res = subprocess.run([sys.executable, os.path.join(ROOT, "tests", "bounds_cases.py"), out], cwd=ROOT, env=env,
+                         stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=900)
+    print(res.stdout[-4000:])
+    assert res.returncode == 0, res.stdout[-4000:]
+    d = np.load(out)
+    return json.loads(str(d["summary"])), d
+
+
+def test_no_case_records_a_violation(checked_run):
+    summary, _ = checked_run
+    for name, *_ in B.CASES:
+        assert summary[name]["violations"] == 0, (name, summary[name])
+
+
+def test_checks_see_a_shrunk_buffer(checked_run):
+    summary, _ = checked_run
+    for name in B.SHRINK:
+        s = summary[name + "_shrunk"]
+        assert s["violations"] > 0 and s["site"] in ("spectra store", "spectra load"), (name, s)
+        r = summary[name + "_restored"]
+        assert r["violations"] == 0 and r["same"], (name, r)
+
+
+@pytest.mark.parametrize("i", range(len(B.CASES)), ids=[c[0] for c in B.CASES])
+def test_checked_equals_unchecked_and_oracle(checked_run, i):
+    from powerfit_gb300 import _lib
+    assert not _lib.bounds_checked()
+    _, d = checked_run
+    name, shape, kind, nrot, flags, _ = B.CASES[i]
+    lcc, rot, rmax = B.run_case(_lib, i)
+    c_lcc, c_rot = d[name + "_lcc"], d[name + "_rot"]
+    diff = np.abs(c_lcc.astype(np.float64) - lcc)
+    assert np.max(diff) <= 1e-6, (name, float(np.max(diff)))
+    same = diff == 0
+    assert np.array_equal(c_rot[same], rot[same]), name
+    if rmax is not None:
+        assert np.max(np.abs(d[name + "_rotmax"] - rmax)) <= 1e-6
+    if kind == "rand":
+        target, template, mask, rots = B.build_case(shape, kind, nrot, 100 + i)
+        p = O.prepare(target, template, mask, False)
+        ref, ref_rot, second = O.scan(p, rots, track_second=True)
+        fin = np.isfinite(ref)
+        assert np.array_equal(np.isfinite(c_lcc), fin), name
+        assert np.max(np.abs(c_lcc[fin] - ref[fin])) < 1e-4, name
+        clear = fin & ((ref - second) > 1e-4)
+        assert np.array_equal(c_rot[clear], ref_rot[clear]), name

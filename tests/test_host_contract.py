@@ -176,6 +176,26 @@ def test_library_exports_every_header_symbol():
     assert sorted(_lib.EXPORTS) == syms
 
 
+def test_checked_variant_exports_the_same_symbols():
+    """The bounds-checked build exports the same C ABI and says which build it
+    is; the unchecked build refuses its debugging calls (no device needed)."""
+    import ctypes
+    from powerfit_gb300 import build
+    try:
+        paths = build.build_variants(("", "checked"))
+    except Exception as e:  # no nvcc
+        pytest.skip("cannot build the CUDA library here: %s" % e)
+    plain, checked = (ctypes.CDLL(p) for p in paths)
+    for s in _header_symbols():
+        assert hasattr(checked, s), s
+    assert checked.pf_bounds_checked() == 1 and plain.pf_bounds_checked() == 0
+    a, b = ctypes.c_uint64(7), ctypes.c_uint64(7)
+    plain.pf_debug_bounds.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+    assert plain.pf_debug_bounds(0, ctypes.byref(a), ctypes.byref(b)) == -6
+    plain.pf_debug_buffer_extent.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+    assert plain.pf_debug_buffer_extent(None, 5) == -1
+
+
 def test_host_splat_matches_reference_outputs():
     d = np.load(os.path.join(ROOT, "tests", "golden", "prep.npz"))
     for wrap in (1, 0):
