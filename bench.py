@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--precision", action="store_true",
                     help="precision study: GPU variants vs the float64 oracle on a rotation subset")
     ap.add_argument("--precision-rotations", type=int, default=32)
+    ap.add_argument("--precision-timed", type=int, default=2048, help="rotations of each variant's speed run")
     return ap.parse_args()
 
 
@@ -505,8 +506,11 @@ def run_queue(args):
 
 def run_precision(args):
     """Precision study: max |dLCC| and argmax agreement of the GPU variants
-    (float32 FFTs with float-float or float64 normalisation) against the
-    float64 oracle, on a rotation subset of the configuration."""
+    against the float64 oracle, on a rotation subset of the configuration:
+    float32 FFTs with float-float or float64 normalisation, and the DFT stages
+    on the tensor cores in split-bf16x3 (PF_FLAG_TENSOR_DFT; runtime-planned
+    kernels).  Each variant's search speed is timed on a larger slice, next to
+    the float32 runtime-planned kernels it replaces."""
     import multiprocessing as mp
     cores = os.cpu_count() or 1
     pool = mp.get_context("spawn").Pool(cores)
@@ -533,7 +537,11 @@ def run_precision(args):
         rrot = np.where(better, pr + off, rrot)
     oracle_s = time.perf_counter() - t0
     res = {}
-    for name, flags in (("fp32_fft+floatfloat_norm", 0), ("fp32_fft+fp64_norm", _lib.PF_FLAG_FP64_NORM)):
+    timed = rot[:min(rot.shape[0], args.precision_timed)]
+    variants = (("fp32_fft+floatfloat_norm", 0), ("fp32_fft+fp64_norm", _lib.PF_FLAG_FP64_NORM),
+                ("fp32_fft_runtime_planned+floatfloat_norm", _lib.PF_FLAG_GENERIC),
+                ("bf16x3_tensor_dft+floatfloat_norm", _lib.PF_FLAG_TENSOR_DFT))
+    for name, flags in variants:
         corr = CUDACorrelator(target, laplace=cfg["laplace"], flags=flags)
         corr.template = template
         corr.mask = mask
@@ -545,10 +553,17 @@ def run_precision(args):
         agree = float(np.mean(corr.rot[clear] == rrot[clear])) if clear.any() else 1.0
         res[name] = {"max_abs_dlcc": err, "argmax_agreement_where_gap_gt_1e-4": agree,
                      "clear_voxels": int(clear.sum())}
+        ctx = corr.context            # speed on a larger slice (device-resident, one warm-up)
+        ctx.set_rotations(timed)
+        ctx.scan_resident(0, min(64, timed.shape[0]), flags=flags)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        ctx.scan_resident(0, timed.shape[0], flags=flags)
+        ctx.synchronize()
+        res[name]["rotations_per_s"] = timed.shape[0] / (time.perf_counter() - t0)
     line = {"metric": "precision vs float64 oracle", "config": {"workload": args.config, "grid": list(target.shape),
             "rotations": int(sub.shape[0]), "laplace": cfg["laplace"], "core_weighted": cfg["core_weighted"]},
-            "variants": res, "oracle_s": oracle_s, "oracle_cores": cores,
-            "note": "a split-bf16x3 tensor-core DFT variant is not built: the path is HBM- and latency-bound"}
+            "variants": res, "oracle_s": oracle_s, "oracle_cores": cores, "timed_rotations": int(timed.shape[0])}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -564,7 +579,8 @@ def run_kernels(args):
     """One launch of every kernel outside the fast search passes, at 128^3:
     GPU preprocessing (splat, dilation, Laplace, core weights), the
     runtime-planned search passes and target spectra (PF_FLAG_GENERIC), the
-    float64 unit mirrors, the shard merge and the proposal network's kernels.
+    same passes with the DFT stages on the tensor cores (PF_FLAG_TENSOR_DFT),
+    the float64 unit mirrors, the shard merge and the proposal network's kernels.
     Wall time per call (synchronised); meant as the command an ncu capture
     of these kernels runs."""
     import torch
@@ -603,6 +619,7 @@ def run_kernels(args):
     ctx.set_template_mask(base._template, base._mask, float(base._norm_factor), base._rmax)
     rot = quat_to_rotmat(super_fibonacci(8))
     timed("scan generic", lambda: ctx.scan(rot, flags=_lib.PF_FLAG_GENERIC))
+    timed("scan tensor-core DFT", lambda: ctx.scan(rot, flags=_lib.PF_FLAG_TENSOR_DFT))
     lcc, r = ctx.scan(rot[:2])
     timed("combine", lambda: _lib.combine_into(lcc.copy(), r.copy(), lcc, r, 0))
     timed("fft3d", lambda: ctx.fft3d(target.astype(np.float32)))

@@ -41,6 +41,8 @@ extern "C" {
 #define PF_FLAG_ACCUMULATE 4  /* keep the running best of earlier scans (do not reset) */
 #define PF_FLAG_GENERIC 8     /* use the runtime-planned kernels even where a specialised path exists */
 #define PF_FLAG_ROT_MAX 16    /* also keep, per rotation, the best LCC over the lcc-mask voxels (pf_get_rotation_max) */
+#define PF_FLAG_TENSOR_DFT 32 /* precision study: the DFT stages of the search on the tensor cores in split-bf16x3
+                                 (mma.sync bf16, float32 accumulation; runtime-planned kernels, edges <= 256) */
 
 typedef struct pf_ctx pf_ctx;
 

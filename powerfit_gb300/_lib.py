@@ -26,6 +26,7 @@ PF_FLAG_NO_PRUNE = 2
 PF_FLAG_ACCUMULATE = 4
 PF_FLAG_GENERIC = 8
 PF_FLAG_ROT_MAX = 16
+PF_FLAG_TENSOR_DFT = 32
 
 EXPORTS = [
     "pf_create", "pf_destroy", "pf_last_error", "pf_global_error", "pf_set_target",

@@ -339,12 +339,17 @@ int set_smem_limits(pf_ctx* c) {
   // allow every kernel the device's opt-in maximum (static + dynamic); a
   // launch only takes what it asks for
   const size_t m = c->max_smem;
-  PF_CUDA(c, allow_smem(k_pass1, m));
-  PF_CUDA(c, allow_smem(k_pass3, m));
+  PF_CUDA(c, allow_smem(k_pass1<false>, m));
+  PF_CUDA(c, allow_smem(k_pass3<false>, m));
   PF_CUDA(c, allow_smem(k_fwd_x_real, m));
-  PF_CUDA(c, allow_smem(k_pass2, m));
-  PF_CUDA(c, allow_smem(k_split_rows, m));
-  PF_CUDA(c, allow_smem(k_split_cols, m));
+  PF_CUDA(c, allow_smem(k_pass2<false>, m));
+  PF_CUDA(c, allow_smem(k_split_rows<false>, m));
+  PF_CUDA(c, allow_smem(k_split_cols<false>, m));
+  PF_CUDA(c, allow_smem(k_pass1<true>, m));
+  PF_CUDA(c, allow_smem(k_pass3<true>, m));
+  PF_CUDA(c, allow_smem(k_pass2<true>, m));
+  PF_CUDA(c, allow_smem(k_split_rows<true>, m));
+  PF_CUDA(c, allow_smem(k_split_cols<true>, m));
   if (c->fast) PF_CUDA(c, c->fl.set_attrs(m, m));
   return PF_OK;
 }
@@ -400,23 +405,32 @@ int upload_double_as_float(pf_ctx* c, float* dst, const double* src, long long n
 constexpr int kSplitRows = 16;   // rows per tile of the split pass 2 (steps 2a, 2c)
 constexpr int kSplitCols = 16;   // columns per tile (step 2b)
 
-// pass 2 in three steps through global memory (planes larger than shared memory)
-int launch_split_pass2(pf_ctx* c, const Geometry& g, int npairs, int nfield, int mode, float2* out, float scale) {
+// pass 2 in three steps through global memory (planes larger than shared memory);
+// tc: DFT stages on the tensor cores (split-bf16x3)
+// The tensor-core stages hold at most 8 * kMmaGroups butterflies per warp in a
+// chunk: with 256-thread blocks a line of nb = L/R <= 128 butterflies always fits.
+constexpr int kTensorDftMaxEdge = 256;
+
+int launch_split_pass2(pf_ctx* c, const Geometry& g, int npairs, int nfield, int mode, float2* out, float scale,
+                       bool tc = false) {
   const size_t srow = ((size_t)c->ny + (size_t)kSplitRows * (c->ny + kPad)) * sizeof(float2);
   const size_t scol = ((size_t)c->nz + (size_t)c->nz * (kSplitCols + kPad)) * sizeof(float2);
   SplitRowsParams pr{g, c->py, c->twy, c->buf, nfield, kSplitRows, 0, buf_extent(c)};
   dim3 gr((g.nvz + kSplitRows - 1) / kSplitRows, c->nx, npairs * nfield);
-  k_split_rows<<<gr, kThreadsLine, srow, c->stream>>>(pr);
+  if (tc) k_split_rows<true><<<gr, kThreadsLine, srow, c->stream>>>(pr);
+  else k_split_rows<false><<<gr, kThreadsLine, srow, c->stream>>>(pr);
   PF_CUDA(c, cudaGetLastError());
   SplitColsParams pc{g, c->pz, c->twz, c->buf, c->spec, c->spec + c->N, nfield, kSplitCols, mode, out, scale,
                      buf_extent(c), c->N, out ? 2 * c->N : 0};
   dim3 gc((c->ny + kSplitCols - 1) / kSplitCols, c->nx, npairs * nfield);
-  k_split_cols<<<gc, kThreadsLine, scol, c->stream>>>(pc);
+  if (tc) k_split_cols<true><<<gc, kThreadsLine, scol, c->stream>>>(pc);
+  else k_split_cols<false><<<gc, kThreadsLine, scol, c->stream>>>(pc);
   PF_CUDA(c, cudaGetLastError());
   if (mode == 0) {
     SplitRowsParams pi{g, c->py, c->twy, c->buf, nfield, kSplitRows, 1, buf_extent(c)};
     dim3 gi((c->nz + kSplitRows - 1) / kSplitRows, c->nx, npairs * nfield);
-    k_split_rows<<<gi, kThreadsLine, srow, c->stream>>>(pi);
+    if (tc) k_split_rows<true><<<gi, kThreadsLine, srow, c->stream>>>(pi);
+    else k_split_rows<false><<<gi, kThreadsLine, srow, c->stream>>>(pi);
     PF_CUDA(c, cudaGetLastError());
   }
   return PF_OK;
@@ -454,7 +468,7 @@ int forward_two_fields(pf_ctx* c, const float* in0, const float* in1, int square
   } else if (c->fast) {
     c->fl.pass2(p2, 0, g2, plane_smem(c->ny, c->nz), c->stream);
   } else {
-    k_pass2<<<g2, kThreadsPlane, plane_smem(c->ny, c->nz), c->stream>>>(p2);
+    k_pass2<false><<<g2, kThreadsPlane, plane_smem(c->ny, c->nz), c->stream>>>(p2);
   }
   PF_CUDA(c, cudaGetLastError());
   PF_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -755,6 +769,8 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
   if (!c->have_target || !c->have_template) return fail(c, PF_E_STATE, "set the target and the template/mask first");
   if (first < 0 || count < 0 || first + count > c->nrot) return fail(c, PF_E_ARG, "rotation range outside the uploaded set");
   if (rot_offset + first + count > (int64_t)0x7fffffff) return fail(c, PF_E_ARG, "rotation index overflows int32");
+  if ((flags & PF_FLAG_TENSOR_DFT) && std::max(c->nx, std::max(c->ny, c->nz)) > kTensorDftMaxEdge)
+    return fail(c, PF_E_ARG, "PF_FLAG_TENSOR_DFT: grid edges are limited to %d", kTensorDftMaxEdge);
   DeviceGuard guard(c->device);
   int rc = ensure_buf(c, c->pairs);
   if (rc) return rc;
@@ -787,7 +803,8 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
   const int P = c->pairs;
   const int ty1 = c->ty1, ty3 = c->ty3;
   const size_t s1 = line_smem(c->nx, 3, ty1), s3 = line_smem(c->nx, 3, ty3), s2 = plane_smem(c->ny, c->nz);
-  const bool fast = c->fast && !(flags & PF_FLAG_GENERIC);
+  const bool tc = (flags & PF_FLAG_TENSOR_DFT) != 0;
+  const bool fast = c->fast && !(flags & PF_FLAG_GENERIC) && !tc;
   const int re = std::min(g.rmax, g.reff);
   const int re2 = re * re;
   const int64_t end = first + count;
@@ -804,7 +821,8 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
         return 1;
       } else {
         dim3 g1(g.nvz, (c->ny + ty1 - 1) / ty1, npairs);
-        k_pass1<<<g1, kThreadsLine, s1, c->stream>>>(p1);
+        if (tc) k_pass1<true><<<g1, kThreadsLine, s1, c->stream>>>(p1);
+        else k_pass1<false><<<g1, kThreadsLine, s1, c->stream>>>(p1);
         return 1;
       }
     });
@@ -829,10 +847,11 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
         return 1;
       }
       if (c->split) {
-        launch_split_pass2(c, g, npairs, 3, 0, nullptr, 1.0f);   // rows, columns, rows
+        launch_split_pass2(c, g, npairs, 3, 0, nullptr, 1.0f, tc);   // rows, columns, rows
         return 3;
       }
-      k_pass2<<<g2, kThreadsPlane, s2, c->stream>>>(p2);
+      if (tc) k_pass2<true><<<g2, kThreadsPlane, s2, c->stream>>>(p2);
+      else k_pass2<false><<<g2, kThreadsPlane, s2, c->stream>>>(p2);
       return 1;
     });
     if (rc) return rc;
@@ -868,7 +887,8 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
             c->part_lcc, c->part_rot, 0, c->lcc, c->rot, c->N);
         return 2;
       }
-      k_pass3<<<g3, kThreadsLine, s3, c->stream>>>(p3);
+      if (tc) k_pass3<true><<<g3, kThreadsLine, s3, c->stream>>>(p3);
+      else k_pass3<false><<<g3, kThreadsLine, s3, c->stream>>>(p3);
       return 1;
     });
     if (rc) return rc;
@@ -1216,9 +1236,9 @@ int pf_scan_noalloc(int nz, int ny, int nx, const float* d_target, const uint8_t
 
   // kernel attributes (idempotent) and twiddles (host tables, as for contexts)
   const size_t m = prop.sharedMemPerBlockOptin;
-  PF_CUDA(nullptr, allow_smem(k_pass1, m));
-  PF_CUDA(nullptr, allow_smem(k_pass2, m));
-  PF_CUDA(nullptr, allow_smem(k_pass3, m));
+  PF_CUDA(nullptr, allow_smem(k_pass1<false>, m));
+  PF_CUDA(nullptr, allow_smem(k_pass2<false>, m));
+  PF_CUDA(nullptr, allow_smem(k_pass3<false>, m));
   PF_CUDA(nullptr, allow_smem(k_fwd_x_real, m));
   float2 tw_host[3][kNoAllocMaxEdge];   // same tables as the contexts build (twiddles())
   const int edges[3] = {nx, ny, nz};
@@ -1263,7 +1283,7 @@ int pf_scan_noalloc(int nz, int ny, int nx, const float* d_target, const uint8_t
   pt.scale = (float)(1.0 / (double)N);
   pt.buf_len = buf_len;
   pt.out_len = 2 * N;
-  k_pass2<<<dim3(nx, 2, 1), kThreadsPlane, plane_smem(ny, nz), s>>>(pt);
+  k_pass2<false><<<dim3(nx, 2, 1), kThreadsPlane, plane_smem(ny, nz), s>>>(pt);
   PF_CUDA(nullptr, cudaGetLastError());
 
   // the outputs start at zero (strict > against 0, rotation 0)
@@ -1278,7 +1298,7 @@ int pf_scan_noalloc(int nz, int ny, int nx, const float* d_target, const uint8_t
     for (int64_t r0 = 0; r0 < cn; r0 += 2) {
       Pass1Params p1{g, px, GatherSrc{d_tmpl, d_mask}, twx, rots, d_rotmats + 9 * c0, r0, cn, buf, ty1, nullptr, 0,
                      buf_len};
-      k_pass1<<<dim3(nz, (ny + ty1 - 1) / ty1, 1), kThreadsLine, line_smem(nx, 3, ty1), s>>>(p1);
+      k_pass1<false><<<dim3(nz, (ny + ty1 - 1) / ty1, 1), kThreadsLine, line_smem(nx, 3, ty1), s>>>(p1);
       Pass2Params p2{};
       p2.g = g;
       p2.py = py;
@@ -1292,11 +1312,11 @@ int pf_scan_noalloc(int nz, int ny, int nx, const float* d_target, const uint8_t
       p2.mode = 0;
       p2.buf_len = buf_len;
       p2.spec_len = N;
-      k_pass2<<<dim3(nx, 3, 1), kThreadsPlane, plane_smem(ny, nz), s>>>(p2);
+      k_pass2<false><<<dim3(nx, 3, 1), kThreadsPlane, plane_smem(ny, nz), s>>>(p2);
       Pass3Params p3{g, px, twx, buf, 1, r0, cn, rot_offset + c0, d_lcc_mask, (float)norm_factor,
                      d_lcc, d_rot, ty3, 0};
       p3.buf_len = buf_len;
-      k_pass3<<<dim3(nz, (ny + ty3 - 1) / ty3, 1), kThreadsLine, line_smem(nx, 3, ty3), s>>>(p3);
+      k_pass3<false><<<dim3(nz, (ny + ty3 - 1) / ty3, 1), kThreadsLine, line_smem(nx, 3, ty3), s>>>(p3);
       PF_CUDA(nullptr, cudaGetLastError());
     }
   }

@@ -69,8 +69,9 @@ __device__ __forceinline__ bool check_smem(int site, const void* p, int bytes) {
 
 #else
 
-#define PF_CHECK(site, index, n) true
-#define PF_CHECK_SMEM(site, ptr, bytes) true
+// (the operands are named, not evaluated, so that a value used only in checks is not "unused")
+#define PF_CHECK(site, index, n) ((void)sizeof(index), (void)sizeof(n), true)
+#define PF_CHECK_SMEM(site, ptr, bytes) ((void)sizeof(ptr), true)
 
 #endif  // PF_BOUNDS_CHECK
 

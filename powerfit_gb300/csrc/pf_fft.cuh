@@ -300,12 +300,14 @@ __device__ __forceinline__ void fft_stage(int nlines, int L, int Ns, const float
         const int j = it / cl;
 #pragma unroll
         for (int r = 0; r < R; ++r) v[k][r] = src.load(line, j + r * nb);
-        const int jm = (j % Ns) * twmul;
+        if (Ns > 1) {   // (the first stage's twiddles are all 1)
+          const int jm = (j % Ns) * twmul;
 #pragma unroll
-        for (int r = 1; r < R; ++r) {
-          float2 w = PF_CHECK(kChkTwiddle, r * jm, L) ? tw[r * jm] : make_float2(1.f, 0.f);
-          if (INV) w.y = -w.y;
-          v[k][r] = cmul(v[k][r], w);
+          for (int r = 1; r < R; ++r) {
+            float2 w = PF_CHECK(kChkTwiddle, r * jm, L) ? tw[r * jm] : make_float2(1.f, 0.f);
+            if (INV) w.y = -w.y;
+            v[k][r] = cmul(v[k][r], w);
+          }
         }
         DFT<R, INV>::run(v[k]);
       }
@@ -326,9 +328,22 @@ __device__ __forceinline__ void fft_stage(int nlines, int L, int Ns, const float
   }
 }
 
-template <bool INV, int EMAX, class Src, class Dst>
+// split-bf16x3 tensor-core stage (pf_fft_mma.cuh)
+template <bool INV, class Src, class Dst>
+__device__ __noinline__ void fft_stage_mma(int R, int nlines, int L, int Ns, const float2* __restrict__ tw,
+                                           const Src src, const Dst dst, bool alias);
+
+// TC: the R-point DFTs on the tensor cores in split-bf16x3 (a precision-study
+// variant), else in float32 codelets
+template <bool INV, int EMAX, bool TC, class Src, class Dst>
 __device__ __noinline__ void fft_stage_rt(int R, int nlines, int L, int Ns, const float2* __restrict__ tw,
                                           const Src src, const Dst dst, bool alias) {
+  if constexpr (TC) {
+    if (R > 1) {
+      fft_stage_mma<INV>(R, nlines, L, Ns, tw, src, dst, alias);
+      return;
+    }
+  }
   switch (R) {
     case 16: fft_stage<16, INV, EMAX>(nlines, L, Ns, tw, src, dst, alias); break;
     case 12: fft_stage<12, INV, EMAX>(nlines, L, Ns, tw, src, dst, alias); break;
@@ -347,21 +362,21 @@ __device__ __noinline__ void fft_stage_rt(int R, int nlines, int L, int Ns, cons
 // Full transform of `nlines` lines of length pl.n: the first stage reads from
 // `src`, the last writes to `dst`, intermediate stages work in `mid` (shared
 // memory).  `src_alias`/`dst_alias`: whether src/dst share storage with `mid`.
-template <bool INV, int EMAX, class Src, class Mid, class Dst>
+template <bool INV, int EMAX, bool TC = false, class Src, class Mid, class Dst>
 __device__ __forceinline__ void fft_lines(const AxisPlan& pl, int nlines, const float2* __restrict__ tw,
                                           const Src src, const Mid mid, const Dst dst,
                                           bool src_alias, bool dst_alias) {
   int Ns = 1;
   const int L = pl.n;
   if (pl.nst == 1) {
-    fft_stage_rt<INV, EMAX>(pl.radix[0], nlines, L, 1, tw, src, dst, src_alias || dst_alias);
+    fft_stage_rt<INV, EMAX, TC>(pl.radix[0], nlines, L, 1, tw, src, dst, src_alias || dst_alias);
     return;
   }
   for (int s = 0; s < pl.nst; ++s) {
     const int R = pl.radix[s];
-    if (s == 0) fft_stage_rt<INV, EMAX>(R, nlines, L, Ns, tw, src, mid, src_alias);
-    else if (s == pl.nst - 1) fft_stage_rt<INV, EMAX>(R, nlines, L, Ns, tw, mid, dst, dst_alias);
-    else fft_stage_rt<INV, EMAX>(R, nlines, L, Ns, tw, mid, mid, true);
+    if (s == 0) fft_stage_rt<INV, EMAX, TC>(R, nlines, L, Ns, tw, src, mid, src_alias);
+    else if (s == pl.nst - 1) fft_stage_rt<INV, EMAX, TC>(R, nlines, L, Ns, tw, mid, dst, dst_alias);
+    else fft_stage_rt<INV, EMAX, TC>(R, nlines, L, Ns, tw, mid, mid, true);
     Ns *= R;
     __syncthreads();
   }

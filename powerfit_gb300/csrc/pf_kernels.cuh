@@ -26,6 +26,7 @@
 #include <stdint.h>
 
 #include "pf_fft.cuh"
+#include "pf_fft_mma.cuh"
 
 namespace pf {
 
@@ -210,6 +211,8 @@ struct TransposedStore {  // line = f*ty + r  (row y0 + r of field f); idx = kx
 };
 
 #ifdef PF_GENERIC_KERNELS
+// TC (here and below): DFT stages in split-bf16x3 on the tensor cores (pf_fft_mma.cuh)
+template <bool TC>
 __global__ void __launch_bounds__(kThreadsLine) k_pass1(const Pass1Params p) {
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
@@ -253,7 +256,7 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass1(const Pass1Params p) {
   SmemLines lines{fld, rs, 1};
   const long long pair_off = (long long)pair * 3 * g.nx * g.nz * g.ny;
   TransposedStore out{p.buf + pair_off, p.ty, y0, g.ny, g.nz, g.nx, z, p.buf_len - pair_off};
-  fft_lines<false, kEmax>(p.px, 3 * p.ty, tw, lines, lines, out, true, false);
+  fft_lines<false, kEmax, TC>(p.px, 3 * p.ty, tw, lines, lines, out, true, false);
 }
 
 #endif  // PF_GENERIC_KERNELS
@@ -306,6 +309,7 @@ struct ProductStore {  // column transforms: line = ky, idx = kz
 };
 
 #ifdef PF_GENERIC_KERNELS
+template <bool TC>
 __global__ void __launch_bounds__(kThreadsPlane) k_pass2(const Pass2Params p) {
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
@@ -335,22 +339,22 @@ __global__ void __launch_bounds__(kThreadsPlane) k_pass2(const Pass2Params p) {
   __syncthreads();
 
   RowMapLines rows{pl, rs, g.zlo, Z - nvz};
-  fft_lines<false, kEmax>(p.py, nvz, twy, rows, rows, rows, true, true);
+  fft_lines<false, kEmax, TC>(p.py, nvz, twy, rows, rows, rows, true, true);
   SmemLines cols{pl, 1, rs};
   if (p.mode == 0) {
     const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + (long long)kx * plane;
     ProductStore prod{pl, rs, spec, Y, p.spec_len - (long long)kx * plane};
-    fft_lines<false, kEmax>(p.pz, Y, twz, cols, cols, prod, true, true);
-    fft_lines<true, kEmax>(p.pz, Y, twz, cols, cols, cols, true, true);
+    fft_lines<false, kEmax, TC>(p.pz, Y, twz, cols, cols, prod, true, true);
+    fft_lines<true, kEmax, TC>(p.pz, Y, twz, cols, cols, cols, true, true);
     SmemLines allrows{pl, rs, 1};
-    fft_lines<true, kEmax>(p.py, Z, twy, allrows, allrows, allrows, true, true);
+    fft_lines<true, kEmax, TC>(p.py, Z, twy, allrows, allrows, allrows, true, true);
     for (int v = threadIdx.x; v < Z * Y; v += blockDim.x) {
       const int z = v / Y, y = v - z * Y;
       const long long i = (long long)z * Y + y;
       if (PF_CHECK(kChkBufStore, i, glim) && PF_CHECK_SMEM(kChkSmem, pl + z * rs + y, 8)) gplane[i] = pl[z * rs + y];
     }
   } else {
-    fft_lines<false, kEmax>(p.pz, Y, twz, cols, cols, cols, true, true);
+    fft_lines<false, kEmax, TC>(p.pz, Y, twz, cols, cols, cols, true, true);
     const long long out_off = ((long long)f * g.nx + kx) * plane;
     float2* o = p.out + out_off;
     for (int v = threadIdx.x; v < Z * Y; v += blockDim.x) {
@@ -402,6 +406,7 @@ struct SplitColsParams {
 
 #ifdef PF_GENERIC_KERNELS
 // grid: (row tiles of one (field, kx) plane, kx, pair * nfield + field)
+template <bool TC>
 __global__ void __launch_bounds__(kThreadsLine) k_split_rows(const SplitRowsParams p) {
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
@@ -427,8 +432,8 @@ __global__ void __launch_bounds__(kThreadsLine) k_split_rows(const SplitRowsPara
   }
   __syncthreads();
   SmemLines lines{t, rs, 1};
-  if (p.inverse) fft_lines<true, kEmax>(p.py, nr, tw, lines, lines, lines, true, true);
-  else fft_lines<false, kEmax>(p.py, nr, tw, lines, lines, lines, true, true);
+  if (p.inverse) fft_lines<true, kEmax, TC>(p.py, nr, tw, lines, lines, lines, true, true);
+  else fft_lines<false, kEmax, TC>(p.py, nr, tw, lines, lines, lines, true, true);
   for (int v = threadIdx.x; v < nr * Y; v += blockDim.x) {
     const int l = v / Y, y = v - l * Y;
     const long long i = (long long)row_of(l) * Y + y;
@@ -437,6 +442,7 @@ __global__ void __launch_bounds__(kThreadsLine) k_split_rows(const SplitRowsPara
 }
 
 // grid: (column tiles, kx, pair * nfield + field)
+template <bool TENSOR>
 __global__ void __launch_bounds__(kThreadsLine) k_split_cols(const SplitColsParams p) {
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
@@ -469,8 +475,8 @@ __global__ void __launch_bounds__(kThreadsLine) k_split_cols(const SplitColsPara
     const long long spec_off = (long long)kx * plane + y0;
     const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + spec_off;
     ProductStore prod{t, rs, spec, Y, p.spec_len - spec_off};
-    fft_lines<false, kEmax>(p.pz, nc, tw, cols, cols, prod, true, true);
-    fft_lines<true, kEmax>(p.pz, nc, tw, cols, cols, cols, true, true);
+    fft_lines<false, kEmax, TENSOR>(p.pz, nc, tw, cols, cols, prod, true, true);
+    fft_lines<true, kEmax, TENSOR>(p.pz, nc, tw, cols, cols, cols, true, true);
     for (int v = threadIdx.x; v < Z * TC; v += blockDim.x) {
       const int z = v / TC, c = v - z * TC;
       const long long i = (long long)z * Y + y0 + c;
@@ -478,7 +484,7 @@ __global__ void __launch_bounds__(kThreadsLine) k_split_cols(const SplitColsPara
         gplane[i] = t[z * rs + c];
     }
   } else {
-    fft_lines<false, kEmax>(p.pz, nc, tw, cols, cols, cols, true, true);
+    fft_lines<false, kEmax, TENSOR>(p.pz, nc, tw, cols, cols, cols, true, true);
     const long long out_off = ((long long)f * g.nx + kx) * plane;
     float2* o = p.out + out_off;
     for (int v = threadIdx.x; v < Z * TC; v += blockDim.x) {
@@ -613,6 +619,7 @@ constexpr int kMaxVoxPass3Fast = PF_PASS3_MAXVOX;
 constexpr int kPass3BlocksPerSm = PF_PASS3_MINB;
 
 #ifdef PF_GENERIC_KERNELS
+template <bool TC>
 __global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {
   extern __shared__ float2 sm[];
   __shared__ unsigned long long s_red[64];
@@ -622,6 +629,7 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {
   float2* fld = sm + X;                      // [3][ty][X + kPad]
   const int rs = X + kPad;
   for (int i = threadIdx.x; i < X; i += blockDim.x) tw[i] = p.twx[i];
+  __syncthreads();   // the twiddle table is read before the first barrier of the transform
 
   const int z = blockIdx.x;
   const int y0 = blockIdx.y * p.ty;
@@ -653,7 +661,7 @@ __global__ void __launch_bounds__(kThreadsLine) k_pass3(const Pass3Params p) {
     GlobalRowsLoad src{p.buf + (long long)pair * 3 * fstride, p.ty, y0, g.ny, g.nz, g.nx, z,
                        p.buf_len - (long long)pair * 3 * fstride};
     SmemLines lines{fld, rs, 1};
-    fft_lines<true, kEmax>(p.px, 3 * p.ty, tw, src, lines, lines, false, true);
+    fft_lines<true, kEmax, TC>(p.px, 3 * p.ty, tw, src, lines, lines, false, true);
     __syncthreads();
     const long long ra = p.first_rot + 2LL * pair;
     const bool has_b = ra + 1 < p.nrot;

@@ -19,6 +19,9 @@ pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 LCC_TOL = 1e-4
 GAP_TOL = 1e-4
+# precision-study variant (split-bf16x3 tensor-core DFT stages): held to the
+# parity tolerance (measured on a GB300: 1.1e-5 to 1.8e-5, float32 stages 3e-7 to 6e-7)
+TENSOR_DFT_LCC_BOUND = LCC_TOL
 
 
 @pytest.fixture(scope="module")
@@ -262,6 +265,33 @@ def test_autotune_keeps_results(lib):
     assert cfg["rows3"] & (cfg["rows3"] - 1) == 0
     lcc, r = ctx.scan(rot)
     assert np.array_equal(lcc, base.lcc) and np.array_equal(r, base.rot)
+
+
+@pytest.mark.parametrize("shape", [(48, 48, 48), (40, 36, 30), (192, 192, 12)])
+def test_tensor_dft_variant_against_oracle(lib, shape):
+    """The precision-study variant with the DFT stages on the tensor cores in
+    split-bf16x3 (PF_FLAG_TENSOR_DFT): a correct search (the LCC against the
+    oracle within the bound below, the argmax where the oracle's top-two gap
+    exceeds 1e-4), less precise than the float32 stages it replaces."""
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    from powerfit_gb300._lib import PF_FLAG_GENERIC, PF_FLAG_TENSOR_DFT
+    from powerfit_gb300 import synth
+    c = synth.make_case(shape, 2.0, 500, 2, 8.0, 5.0, 31)
+    rot = quat_to_rotmat(super_fibonacci(96))[::8]
+    target = c.target.astype(np.float64)
+    p = O.prepare(target, c.template, c.mask, False)
+    ref, ref_rot, second = O.scan(p, rot, track_second=True)
+    corr = correlator(target, c.template, c.mask, rot, False, flags=PF_FLAG_TENSOR_DFT)
+    fin = np.isfinite(ref)
+    err_tc = float(np.max(np.abs(corr.lcc[fin] - ref[fin])))
+    clear = fin & ((ref - second) > 1e-4) & (ref > 0)
+    agree = float(np.mean(corr.rot[clear] == ref_rot[clear]))
+    lg, _ = corr.context.scan(rot, flags=PF_FLAG_GENERIC)
+    err_fp32 = float(np.max(np.abs(lg[fin] - ref[fin])))
+    print("%s tensor-core split-bf16x3 max|dLCC| %.2e, argmax %.5f of %d clear voxels; float32 %.2e"
+          % (shape, err_tc, agree, int(clear.sum()), err_fp32))
+    assert err_tc < TENSOR_DFT_LCC_BOUND and agree >= 0.999
+    assert err_fp32 <= err_tc
 
 
 def test_split_plane_path_vs_oracle(lib):
