@@ -14,8 +14,9 @@ The cases cover every kernel family of the search: the runtime-planned
 kernels on tiny and odd grids (4x5x6, 5x6x7, 8^3, 10x12x14, 15x16x21,
 40x48x36), the compile-time kernels of every specialised size (32 .. 160),
 the clustered plane pass (192^3), the three-step plane pass (192x192x12),
-pruning on and off, the per-rotation maxima, float64 normalisation, and
-batch and tile shapes other than the defaults.
+pruning on and off, the per-rotation maxima, float64 normalisation, the
+tensor-core DFT stages of the precision study, and batch and tile shapes
+other than the defaults.
 """
 from __future__ import annotations
 
@@ -29,7 +30,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-FP64, NO_PRUNE, GENERIC, ROT_MAX = 1, 2, 8, 16
+FP64, NO_PRUNE, GENERIC, ROT_MAX, TENSOR_DFT = 1, 2, 8, 16, 32
 
 # name, shape, inputs ("rand": uniform noise, "synth": seeded map), rotations,
 # flags, tuning (pairs per batch, pass-1 rows, pass-3 rows; 0: default) or None
@@ -49,6 +50,8 @@ CASES = [
     ("fast160", (160, 160, 160), "synth", 8, 0, None),
     ("cluster192", (192, 192, 192), "synth", 6, 0, None),
     ("split_192x192x12", (192, 192, 12), "synth", 6, 0, None),
+    ("tensor_dft_48", (48, 48, 48), "synth", 10, TENSOR_DFT, None),
+    ("tensor_dft_split", (192, 192, 12), "synth", 6, TENSOR_DFT, None),
 ]
 
 # cases re-run with a shrunk buffer extent (the checks must report accesses)
