@@ -146,13 +146,33 @@ def make_pool(n):
 
 def cpu_sample(pool, nproc, target, template, mask, rot, laplace, per_core):
     """Time the reference's _cpu_scan structure on nproc processes over the
-    first nproc*per_core rotations; returns rotations/s."""
+    first nproc*per_core rotations; returns rotations/s, the rotation count,
+    the seconds and the sample's (lcc, rot)."""
     from oracle import oracle as O
     sample = rot[: nproc * per_core]
     t0 = time.perf_counter()
-    O.cpu_scan(target, template, mask, sample, laplace, nproc=nproc, pool=pool)
+    res = O.cpu_scan(target, template, mask, sample, laplace, nproc=nproc, pool=pool)
     dt = time.perf_counter() - t0
-    return sample.shape[0] / dt, sample.shape[0], dt
+    return sample.shape[0] / dt, sample.shape[0], dt, res
+
+
+def precision_vs_oracle(ftarget, base, sample, ref, device):
+    """The GPU search on the CPU baseline's rotation sample against the
+    oracle's result for it (float64): max |dLCC| and argmax agreement."""
+    from powerfit_gb300 import _lib
+    ctx = _lib.Context(ftarget.shape, device)
+    ctx.set_target(ftarget, base._lcc_mask)
+    ctx.set_template_mask(base._template, base._mask, float(base._norm_factor), base._rmax)
+    lcc, rot = ctx.scan(sample)
+    ctx.close()
+    ref_lcc, ref_rot = ref
+    fin = np.isfinite(ref_lcc)
+    hit = fin & (ref_lcc > 0)
+    return {"max_abs_dlcc": float(np.max(np.abs(lcc[fin] - ref_lcc[fin]))),
+            "argmax_agreement": float(np.mean(rot[hit] == ref_rot[hit])) if hit.any() else 1.0,
+            "voxels": int(hit.sum()), "rotations": int(sample.shape[0]), "tolerance": 1e-4,
+            "reference": "float64 oracle (restated CPUCorrelator) on the CPU baseline's sample; argmax over "
+                         "every voxel with a positive best LCC, near-ties included"}
 
 
 def run_reference(args, rank, world):
@@ -167,7 +187,7 @@ def run_reference(args, rank, world):
     vals = []
     tot_rot, tot_t = 0, 0.0
     for _ in range(args.steps):
-        v, n, dt = cpu_sample(pool, cores, target, template, mask, rot, cfg["laplace"], per_core)
+        v, n, dt, _ = cpu_sample(pool, cores, target, template, mask, rot, cfg["laplace"], per_core)
         vals.append(v)
         tot_rot += n
         tot_t += dt
@@ -419,11 +439,13 @@ def run_ours(args, rank, world, local_rank):
                               "pruned_frac": pruned_bytes * value / world / 1e9 / peak},
     }
     if pool is not None:
-        cv, cn, cdt = cpu_sample(pool, cores, target, template, mask, rot_all, cfg["laplace"], args.cpu_rot_per_core)
+        cv, cn, cdt, cres = cpu_sample(pool, cores, target, template, mask, rot_all, cfg["laplace"],
+                                       args.cpu_rot_per_core)
         pool.close()
         line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": "%d rotations (%d per core) of the same workload, %.1f s, "
                                           "_cpu_scan structure with numpy.fft" % (cn, args.cpu_rot_per_core, cdt)}
+        line["precision"] = precision_vs_oracle(ftarget, base, rot_all[:cn], cres, local_rank)
     if args.learned_maps > 0 and world == 1:
         line["learned"] = learned_leg(args.learned_maps)
     print(json.dumps(line), flush=True)
