@@ -81,9 +81,19 @@ constexpr int ct_floor_pow2(int v) {
   return p;
 }
 
+constexpr int ct_log2(int v) {
+  int l = 0;
+  while ((1 << (l + 1)) <= v) ++l;
+  return l;
+}
+
 // One radix-R stage over `nlines` lines of length L.  Lines are processed in
-// chunks of C (a power of two) lines; every item (line, butterfly) of a chunk
-// is loaded into registers before any is stored, so src and dst may alias.
+// chunks of C (a power of two) lines, mapped line-fastest (consecutive threads
+// take consecutive lines); every item (line, butterfly) of a chunk is loaded
+// into registers before any is stored, so src and dst may alias.  A last,
+// partial chunk of at most C/2 lines is mapped as C/2 lines: its items then
+// fill whole warps and the other warps wait at the barrier instead of issuing
+// with half their lanes off (48 lines: 32 + 16).
 template <int R, bool INV, int L, int NS, int NT, int EMAX, class Src, class Dst>
 __device__ __forceinline__ void ct_stage(int nlines, const float2* __restrict__ tw, const Src& src, const Dst& dst,
                                          bool alias) {
@@ -91,6 +101,7 @@ __device__ __forceinline__ void ct_stage(int nlines, const float2* __restrict__ 
   constexpr int KMAX = (EMAX / R) > 0 ? (EMAX / R) : 1;
   constexpr int C0 = (NT * KMAX) / NB;
   constexpr int C = ct_floor_pow2(C0 > 0 ? C0 : 1);
+  constexpr int LOG2C = ct_log2(C);
   constexpr int K = (C * NB + NT - 1) / NT;          // items per thread per chunk
   constexpr int TWMUL = L / (NS * R);
   // The last stage (Ns * R == L) stores every item exactly where it loaded it
@@ -99,12 +110,15 @@ __device__ __forceinline__ void ct_stage(int nlines, const float2* __restrict__ 
   constexpr bool kSelfInPlace = (NS * R == L);
   if (kSelfInPlace) alias = false;
   for (int l0 = 0; l0 < nlines; l0 += C) {
+    // lines this chunk maps: C, or C/2 for a short last chunk
+    const int sh = (C >= 2 && nlines - l0 <= C / 2) ? LOG2C - 1 : LOG2C;
+    const int cm = (1 << sh) - 1;
     float2 v[K][R];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       const int it = threadIdx.x + k * NT;
-      const int line = l0 + (it & (C - 1));
-      const int j = it / C;                          // C is a power of two
+      const int line = l0 + (it & cm);
+      const int j = it >> sh;
       if (j < NB && line < nlines) {
 #pragma unroll
         for (int r = 0; r < R; ++r) v[k][r] = src.load(line, j + r * NB);
@@ -124,8 +138,8 @@ __device__ __forceinline__ void ct_stage(int nlines, const float2* __restrict__ 
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       const int it = threadIdx.x + k * NT;
-      const int line = l0 + (it & (C - 1));
-      const int j = it / C;
+      const int line = l0 + (it & cm);
+      const int j = it >> sh;
       if (j < NB && line < nlines) {
         const int base = (j / NS) * NS * R + (j % NS);
 #pragma unroll
