@@ -142,9 +142,12 @@ __global__ void PF_PASS1_BOUNDS k_pass1_ct(const Pass1Params p, const int re2) {
   // gather the points inside the sphere, spread evenly over the threads
   const int total = s_start[p.ty];
   for (int k = threadIdx.x; k < total; k += kThreadsLine) {
+    // row c of point k: the last row whose start is <= k (starts are
+    // nondecreasing and every listed row holds points), by binary search
     int c = 0;
 #pragma unroll
-    for (int i = 1; i < 32; ++i) c += (i < p.ty && k >= s_start[i]) ? 1 : 0;
+    for (int step = 16; step > 0; step >>= 1)
+      if (c + step < p.ty && s_start[c + step] <= k) c += step;
     const int i = k - s_start[c];
     const int4 e = s_row[c];
     int x, cx;
