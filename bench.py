@@ -230,7 +230,9 @@ def dram_traffic(kernel, n, pairs_per_launch):
     launch's rotation pairs to this run's; (None, reason) without an entry."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
     try:
-        for ln in open(path):
+        with open(path) as f:
+            lines = f.readlines()
+        for ln in lines:
             parts = ln.split()
             if len(parts) >= 5 and not ln.startswith("#") and parts[0] == kernel and int(parts[1]) == n:
                 cap_pairs, rd, wr = int(parts[2]), float(parts[3]), float(parts[4])
@@ -398,7 +400,8 @@ def run_ours(args, rank, world, local_rank):
     avg_s = kms[dom] / 1e3 / max(int(klaunch[dom]), 1)
     peaks = {}
     try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
     except Exception:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))

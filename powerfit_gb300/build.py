@@ -65,7 +65,9 @@ def up_to_date(variant=""):
     if not os.path.exists(lib):
         return False
     try:
-        if open(_stamp(variant)).read() != " ".join(extra_flags()):
+        with open(_stamp(variant)) as f:
+            stamp = f.read()
+        if stamp != " ".join(extra_flags()):
             return False          # built with other variant flags
     except OSError:
         return False

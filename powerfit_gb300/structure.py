@@ -26,7 +26,11 @@ class Structure:
 
     @classmethod
     def fromfile(cls, fid):
-        text = fid.read() if hasattr(fid, "read") else open(fid).read()
+        if hasattr(fid, "read"):
+            text = fid.read()
+        else:
+            with open(fid) as f:
+                text = f.read()
         recs = []
         for line in text.splitlines():
             if not line.startswith(("ATOM  ", "HETATM")):

@@ -73,7 +73,11 @@ def read_map(fid, fmt=None):
     fmt = fmt or os.path.splitext(fname)[-1][1:]
     if fmt not in ("ccp4", "map", "mrc"):
         raise ValueError("Extension of file is not supported.")
-    raw = fid.read() if hasattr(fid, "read") else open(fid, "rb").read()
+    if hasattr(fid, "read"):
+        raw = fid.read()
+    else:
+        with open(fid, "rb") as f:
+            raw = f.read()
     if len(raw) < 1024:
         raise ValueError("file too short for a map header")
     stamp = raw[212]

@@ -25,7 +25,9 @@ def test_bytes_per_rotation_formula():
 
 def test_dram_traffic_scales_with_pairs():
     rows = {}
-    for ln in open(os.path.join(bench.ROOT, "profiles", "dram_traffic.txt")):
+    with open(os.path.join(bench.ROOT, "profiles", "dram_traffic.txt")) as f:
+        lines = f.readlines()
+    for ln in lines:
         if ln.strip() and not ln.startswith("#"):
             p = ln.split()
             rows[(p[0], int(p[1]))] = (int(p[2]), int(p[3]) + int(p[4]))

@@ -155,7 +155,8 @@ def test_synthetic_case_is_seeded():
 
 
 def _header_symbols():
-    text = open(os.path.join(ROOT, "include", "powerfit_gb300.h")).read()
+    with open(os.path.join(ROOT, "include", "powerfit_gb300.h")) as f:
+        text = f.read()
     return sorted(set(re.findall(r"\b(pf_[a-z0-9_]+)\s*\(", text)))
 
 

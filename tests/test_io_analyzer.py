@@ -18,12 +18,17 @@ def test_reads_reference_written_map():
     assert abs(vs - 1.5) < 1e-6 and np.allclose(origin, [3.0, -2.0, 5.0])
 
 
+def _read(path):
+    with open(path, "rb") as f:
+        return f.read()
+
+
 def test_written_map_matches_reference_bytes(tmp_path):
     rng = np.random.default_rng(41)
     arr = rng.random((10, 12, 14)).astype(np.float32).astype(np.float64)
     out = str(tmp_path / "m.mrc")
     write_map(out, Volume(arr, 1.5, np.array([3.0, -2.0, 5.0])))
-    assert open(out, "rb").read() == open(os.path.join(GOLD, "ref_map.mrc"), "rb").read()
+    assert _read(out) == _read(os.path.join(GOLD, "ref_map.mrc"))
 
 
 def test_round_trip_and_axis_order(tmp_path):
@@ -37,7 +42,7 @@ def test_round_trip_and_axis_order(tmp_path):
     # a file stored with sections along x (mapc, mapr, maps = 3, 2, 1)
     path = str(tmp_path / "swap.mrc")
     write_map(path, Volume(arr, 1.0))
-    raw = bytearray(open(path, "rb").read())
+    raw = bytearray(_read(path))
     import struct
     struct.pack_into("<3i", raw, 0, 4, 5, 6)          # nc, nr, ns
     struct.pack_into("<3i", raw, 64, 3, 2, 1)         # mapc, mapr, maps
@@ -45,7 +50,8 @@ def test_round_trip_and_axis_order(tmp_path):
     struct.pack_into("<3f", raw, 40, 6.0, 5.0, 4.0)   # cell lengths (x, y, z)
     data = np.transpose(arr, (2, 1, 0)).astype("<f4").tobytes()   # (x, y, z) sections
     raw[1024:] = data
-    open(path, "wb").write(bytes(raw))
+    with open(path, "wb") as f:
+        f.write(bytes(raw))
     a, _, _ = read_map(path)
     assert np.array_equal(a, arr)
 
@@ -68,5 +74,5 @@ def test_analyzer_matches_reference_solutions(tmp_path):
     assert np.allclose(sols, d["solutions"])
     out = str(tmp_path / "solutions.out")
     an.tofile(out)
-    lines = open(out).read().splitlines()
+    lines = _read(out).decode().splitlines()
     assert lines[0].startswith("#rank") and len(lines) == 1 + len(sols)
