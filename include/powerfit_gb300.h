@@ -33,7 +33,7 @@ extern "C" {
 #define PF_E_NOMEM (-3)     /* device allocation failed */
 #define PF_E_STATE (-4)     /* target / template / rotations not set */
 #define PF_E_SHAPE (-5)     /* grid size not supported (prime factor > 7, plane too large) */
-#define PF_E_UNSUPPORTED (-6) /* not available in this build of the library */
+#define PF_E_UNSUPPORTED (-6) /* not available in this variant of the library */
 
 /* pf_scan flags */
 #define PF_FLAG_FP64_NORM 1   /* local variance and LCC in float64 (default: float-float) */
