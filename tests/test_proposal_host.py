@@ -73,3 +73,37 @@ def test_checkpoint_file_round_trip(tmp_path):
     assert np.array_equal(l2, lcc) and np.array_equal(r2, rot) and (nxt, nrot) == (40, 100)
     checkpoint.save(path, lcc * 2, rot, 60, 100)          # replaced atomically
     assert checkpoint.load(path)[2] == 60
+
+
+def test_best_rank_counts_rotations_scored_above_the_best_fit():
+    from powerfit_gb300 import proposal_train as T
+    fine = np.array([0.10, 0.50, 0.499995, np.nan, 0.30])   # rotation 1 is the best fit; 2 is within 1e-5
+    score = np.array([5.0, 1.0, 4.0, 9.0, 2.0])
+    # rotation 2 counts as the best fit too; 2 rotations (0 and 3) score above it
+    assert T.best_rank(score, fine, 1e-5) == 2
+    assert T.best_rank(score, fine, 1e-7) == 4                 # only rotation 1: 0, 2, 3 and 4 above it
+
+
+def test_summary_of_held_out_rows():
+    from powerfit_gb300 import proposal_train as T
+    rows = []
+    for i, (found, rank) in enumerate([(True, 0), (True, 3), (False, 50)]):
+        row = dict(exhaustive_s=2.0)
+        for name in ("network", "coarse_only"):
+            row[name] = dict(found=found, rank=rank, rank_fraction=rank / 1000.0, time_s=0.5,
+                             found_at={str(f): rank < f * 1000 for f in T.FRACTIONS})
+        rows.append(row)
+    s = T.summarise(rows)
+    assert s["network"]["recall"] == 2 / 3 and s["network"]["time_vs_exhaustive"] == 0.25
+    assert s["network"]["median_rank_fraction"] == 0.003 and s["network"]["worst_rank_fraction"] == 0.05
+    assert s["network"]["recall_at"]["0.005"] == 2 / 3 and s["exhaustive_s"] == 2.0
+
+
+def test_case_parameters_are_seeded_and_in_range():
+    from powerfit_gb300 import proposal_train as T
+    a, b = T.case_params(1234, 96), T.case_params(1234, 96)
+    assert a == b
+    for seed in range(50):
+        p = T.case_params(seed, 96)
+        assert 1000 <= p["natoms"] <= 8000 and 5.0 <= p["resolution"] <= 9.0 and 1.0 <= p["snr"] <= 6.0
+        assert 1 <= p["ncopies"] <= 3 and 1.2 <= p["voxelspacing"] <= 3.0
