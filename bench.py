@@ -51,10 +51,13 @@ def parse():
     ap.add_argument("--config", default="lcc128_filtered")
     ap.add_argument("--rotations", type=int, default=0, help="rotation-set size (default: the config's set)")
     ap.add_argument("--per-step", type=int, default=0, help="rotations per step (default: set size / 8)")
-    ap.add_argument("--cpu-rot-per-core", type=int, default=3)
+    ap.add_argument("--cpu-rot-per-core", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--learned-maps", type=int, default=3,
+    ap.add_argument("--learned-maps", type=int, default=10,
                     help="held-out 128^3 maps for the learned-proposal leg (0: skip)")
+    ap.add_argument("--queue-steps", type=int, default=2,
+                    help="timed steps of the uneven-map queue leg in the default line (0: skip)")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the float64-normalisation leg")
     ap.add_argument("--pairs", type=int, default=0)
     ap.add_argument("--precision", action="store_true",
                     help="precision study: GPU variants vs the float64 oracle on a rotation subset")
@@ -146,24 +149,50 @@ def make_pool(n):
 
 def cpu_sample(pool, nproc, target, template, mask, rot, laplace, per_core):
     """Time the reference's _cpu_scan structure on nproc processes over the
-    first nproc*per_core rotations; returns rotations/s, the rotation count,
-    the seconds and the sample's (lcc, rot)."""
+    first nproc*per_core rotations of `rot`.  Every process times its set-up
+    (the correlator's Laplace filter and target spectra, done once per process
+    in a whole search) apart from its rotation loop, so the rate is the steady
+    state of a whole search: the sample's rotations over the slowest process's
+    loop.  Returns a summary dict and the sample's (lcc, rot)."""
     from oracle import oracle as O
     sample = rot[: nproc * per_core]
     t0 = time.perf_counter()
-    res = O.cpu_scan(target, template, mask, sample, laplace, nproc=nproc, pool=pool)
-    dt = time.perf_counter() - t0
-    return sample.shape[0] / dt, sample.shape[0], dt, res
+    lcc, r, parts = O.cpu_scan_timed(target, template, mask, sample, laplace, nproc=nproc, pool=pool)
+    wall = time.perf_counter() - t0
+    loop = max(pt[1] for pt in parts)
+    n = int(sample.shape[0])
+    return {"value": n / loop, "rotations": n, "loop_s": loop, "wall_s": wall,
+            "prepare_s": statistics.mean(pt[0] for pt in parts), "with_prepare": n / wall}, (lcc, r)
 
 
-def precision_vs_oracle(ftarget, base, sample, ref, device):
+def warm_pool(pool, nproc, target, template, mask, rot, laplace):
+    """One untimed round of one rotation per process: the processes start and
+    import numpy / scipy before the timed sample."""
+    cpu_sample(pool, nproc, target, template, mask, rot, laplace, 1)
+
+
+def sample_rotations(cfg, rot, count):
+    """Rotations of the CPU sample (and of the precision check on it): the
+    reference's own 4.71 degree set where the workload uses that set -- the
+    committed strided slice of c48u2947.npy in tests/golden/rotset_471.npz --
+    else the workload's set."""
+    path = os.path.join(ROOT, "tests", "golden", "rotset_471.npz")
+    if abs(cfg["angle"] - 4.71) < 1e-6 and os.path.exists(path):
+        with np.load(path) as d:
+            ref = d["rotmats"]
+        if ref.shape[0] >= count:
+            return ref[:count], "the reference's 4.71 deg set (every 34th row of c48u2947.npy)"
+    return rot[:count], "the workload's set"
+
+
+def precision_vs_oracle(ftarget, base, sample, ref, device, flags=0):
     """The GPU search on the CPU baseline's rotation sample against the
     oracle's result for it (float64): max |dLCC| and argmax agreement."""
     from powerfit_gb300 import _lib
     ctx = _lib.Context(ftarget.shape, device)
     ctx.set_target(ftarget, base._lcc_mask)
     ctx.set_template_mask(base._template, base._mask, float(base._norm_factor), base._rmax)
-    lcc, rot = ctx.scan(sample)
+    lcc, rot = ctx.scan(sample, flags=flags)
     ctx.close()
     ref_lcc, ref_rot = ref
     fin = np.isfinite(ref_lcc)
@@ -182,28 +211,28 @@ def run_reference(args, rank, world):
     pool = make_pool(cores)
     cfg, target, template, mask, rot, desc = workload(args.config, args.rotations)
     per_core = args.cpu_rot_per_core
-    for _ in range(max(args.warmup, 0) and 1):
-        cpu_sample(pool, cores, target, template, mask, rot[:cores], cfg["laplace"], 1)
-    vals = []
-    tot_rot, tot_t = 0, 0.0
-    for _ in range(args.steps):
-        v, n, dt, _ = cpu_sample(pool, cores, target, template, mask, rot, cfg["laplace"], per_core)
-        vals.append(v)
-        tot_rot += n
-        tot_t += dt
+    sample, sample_src = sample_rotations(cfg, rot, cores * per_core)
+    if args.warmup > 0:
+        warm_pool(pool, cores, target, template, mask, sample, cfg["laplace"])
+    runs = [cpu_sample(pool, cores, target, template, mask, sample, cfg["laplace"], per_core)[0]
+            for _ in range(args.steps)]
     pool.close()
-    value = tot_rot / tot_t
+    tot_rot = sum(r["rotations"] for r in runs)
+    value = tot_rot / sum(r["loop_s"] for r in runs)
     line = {
         "impl": "reference", "metric": metric_for(target.shape), "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(r["wall_s"] for r in runs) / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded map, template, mask; %s)" % desc,
         "config": {"workload": args.config, "grid": list(target.shape), "laplace": cfg["laplace"],
                    "core_weighted": cfg["core_weighted"], "rotation_set_size": int(rot.shape[0]),
                    "sample_rotations_per_step": cores * per_core},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": "first %d rotations per step (%d per core), _cpu_scan structure, numpy.fft"
-                                   % (cores * per_core, per_core)},
+                         "sample": "%d rotations per step (%d per core) from %s, _cpu_scan structure, numpy.fft; "
+                                   "rate over the rotation loops (the per-process set-up, once per process in a "
+                                   "whole search, timed apart)" % (cores * per_core, per_core, sample_src),
+                         "prepare_s": statistics.mean(r["prepare_s"] for r in runs),
+                         "with_prepare": tot_rot / sum(r["wall_s"] for r in runs)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }
@@ -259,8 +288,15 @@ def run_ours(args, rank, world, local_rank):
     cfg, target, template, mask, rot_all, desc = workload(args.config, args.rotations)
     nset = rot_all.shape[0]
     per_step = args.per_step or -(-nset // 8)
-    # weak scaling: every rank scans its own rotations (rank r: set shifted by r * per_step)
-    rot_rank = np.roll(rot_all, -rank * per_step, axis=0)
+    # weak scaling: every rank scans nset rotations of its own, a contiguous
+    # shard of one set of world * nset rotations, stored with their indices in
+    # that set (the shard's first index as the rotation offset)
+    if world > 1:
+        from powerfit_gb300.distributed import weak_scaling_shard
+        from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+        rot_rank, rank_first = weak_scaling_shard(lambda c: quat_to_rotmat(super_fibonacci(c)), nset, rank, world)
+    else:
+        rot_rank, rank_first = rot_all, 0
 
     base = BaseCorrelator(target, laplace=cfg["laplace"])
     base.template = template
@@ -289,13 +325,13 @@ def run_ours(args, rank, world, local_rank):
     geo = ctx.get_geometry()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
-    def step(k, first):
+    def step(k, first, flags=0):
         f = (k * per_step) % nset
         cnt = min(per_step, nset - f)
-        ctx.scan_resident(f, cnt, 0, 0 if first else _lib.PF_FLAG_ACCUMULATE)
+        ctx.scan_resident(f, cnt, rank_first, flags | (0 if first else _lib.PF_FLAG_ACCUMULATE))
         return cnt
 
-    def timed(profile):
+    def timed(profile, flags=0):
         ctx.set_profiling(profile)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
         if world > 1:
@@ -306,7 +342,7 @@ def run_ours(args, rank, world, local_rank):
         for k in range(args.steps):
             flush.zero_()
             ev[k][0].record(stream)
-            done += step(k, k == 0)
+            done += step(k, k == 0, flags)
             ev[k][1].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
@@ -327,6 +363,18 @@ def run_ours(args, rank, world, local_rank):
     # the same steps again with CUDA events around every kernel launch (the
     # per-kernel durations for the roofline)
     _, prof_s, _, kms, klaunch = timed(True)
+    # the same steps with the local variance and the LCC normalisation in
+    # float64 (PF_FLAG_FP64_NORM), the literal precision specification
+    fp64 = None
+    if not args.no_fp64:
+        for w in range(min(args.warmup, 1)):
+            step(w, True, _lib.PF_FLAG_FP64_NORM)
+        torch.cuda.synchronize()
+        f_done, f_s, _, _, _ = timed(False, _lib.PF_FLAG_FP64_NORM)
+        fp64 = {"value": f_done * world / f_s, "unit": UNIT, "ms_per_step": 1e3 * f_s / args.steps,
+                "flags": "PF_FLAG_FP64_NORM",
+                "note": "same workload, steps and timing as the headline; local variance Nm*ave2 - ave^2 and "
+                        "the LCC division in float64 on the GPU (the headline: float-float with FMA products)"}
     t = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -350,7 +398,7 @@ def run_ours(args, rank, world, local_rank):
         ctx.set_target(ftarget, base._lcc_mask)
         ctx.set_template_mask(base._template, base._mask, float(base._norm_factor), base._rmax)
         ctx.set_rotations(rot_host[k])
-        ctx.scan_resident(0, rot_host[k].shape[0], 0, 0)
+        ctx.scan_resident(0, rot_host[k].shape[0], rank_first, 0)
         ctx.get_results(out_lcc, out_rot)
     e2e_s = time.perf_counter() - e0
     te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
@@ -362,10 +410,16 @@ def run_ours(args, rank, world, local_rank):
     d2h = N * 8
 
     # multi-rank: merge per-voxel results on rank 0 (outside the timed region)
+    merged_rot_range = None
     if world > 1:
         from powerfit_gb300 import distributed as D
         lcc_r, rot_r = ctx.get_results()
-        D.gather_and_merge(lcc_r, rot_r, rank_offset=rank * per_step)
+        merged = D.gather_and_merge(lcc_r, rot_r, rank_offset=0)   # indices already global
+        if merged is not None:
+            lo, hi = int(merged[1].min()), int(merged[1].max())
+            if lo < 0 or hi >= world * nset:
+                raise RuntimeError("merged rotation indices [%d, %d] outside [0, %d)" % (lo, hi, world * nset))
+            merged_rot_range = [lo, hi]
 
     if rank != 0:
         return 0
@@ -441,14 +495,28 @@ def run_ours(args, rank, world, local_rank):
                               "pruned_bytes_per_rotation": pruned_bytes,
                               "pruned_frac": pruned_bytes * value / world / 1e9 / peak},
     }
+    if merged_rot_range is not None:
+        line["merged_rotation_range"] = merged_rot_range
+    if fp64 is not None:
+        line["fp64_norm"] = fp64
     if pool is not None:
-        cv, cn, cdt, cres = cpu_sample(pool, cores, target, template, mask, rot_all, cfg["laplace"],
-                                       args.cpu_rot_per_core)
+        sample, sample_src = sample_rotations(cfg, rot_all, cores * args.cpu_rot_per_core)
+        warm_pool(pool, cores, target, template, mask, sample, cfg["laplace"])
+        cs, cres = cpu_sample(pool, cores, target, template, mask, sample, cfg["laplace"], args.cpu_rot_per_core)
         pool.close()
-        line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": "%d rotations (%d per core) of the same workload, %.1f s, "
-                                          "_cpu_scan structure with numpy.fft" % (cn, args.cpu_rot_per_core, cdt)}
-        line["precision"] = precision_vs_oracle(ftarget, base, rot_all[:cn], cres, local_rank)
+        line["cpu_baseline"] = {"value": cs["value"], "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": "%d rotations (%d per core) from %s, same map, template and mask; "
+                                          "_cpu_scan structure with numpy.fft; rate over the rotation loops (%.1f s), "
+                                          "the per-process set-up (once per process in a whole search) timed apart"
+                                          % (cs["rotations"], args.cpu_rot_per_core, sample_src, cs["loop_s"]),
+                                "prepare_s": cs["prepare_s"], "with_prepare": cs["with_prepare"],
+                                "wall_s": cs["wall_s"]}
+        line["precision"] = precision_vs_oracle(ftarget, base, sample, cres, local_rank)
+        line["precision"]["rotations_from"] = sample_src
+        if fp64 is not None:
+            fp64["precision"] = precision_vs_oracle(ftarget, base, sample, cres, local_rank, _lib.PF_FLAG_FP64_NORM)
+    if args.queue_steps > 0 and world == 1:
+        line["queue"] = queue_leg(args.queue_steps, max(1, min(args.warmup, 1)))
     if args.learned_maps > 0 and world == 1:
         line["learned"] = learned_leg(args.learned_maps)
     print(json.dumps(line), flush=True)
@@ -480,51 +548,66 @@ def learned_leg(nmaps):
                        "coarse_grid": [PR.COARSE_EDGE] * 3, "data": "synthetic"}}
 
 
-def run_queue(args):
+def queue_leg(steps, warmup, nrot=0):
     """Uneven-map queue (16 seeded maps of 48^3-160^3, the 9.72 degree set's
-    size): all maps' scans queued on their own streams before any is awaited."""
+    size each): every map's scan queued on its own stream before any is
+    awaited; batch and tile shapes from the autotuner, run once per grid size
+    during the warm-up and reused for every later map of that size.  Also the
+    same queue captured once into one CUDA graph and replayed."""
     import torch
-    from powerfit_gb300.queue import MapJob, make_queue, scan_queue
+    from powerfit_gb300.queue import MapJob, QueueGraph, make_queue, scan_queue
     from powerfit_gb300.rotations import rotation_set
     rot, desc = rotation_set(10.0, data_dir=os.environ.get("POWERFIT_ROTATION_DATA") or "/nonexistent")
-    if args.rotations:
-        rot = rot[:args.rotations]
+    if nrot:
+        rot = rot[:nrot]
     cases = make_queue(16, seed=0)
-    mk = lambda: [MapJob(c.target.astype(np.float64), c.template, c.mask, rot, pairs=128) for c in cases]
-    for _ in range(max(1, args.warmup)):
-        scan_queue(mk(), autotune_trial=0)
+    mk = lambda: [MapJob(c.target.astype(np.float64), c.template, c.mask, rot) for c in cases]
+    tuning = {}
+    t0 = time.perf_counter()
+    for _ in range(max(1, warmup)):
+        scan_queue(mk(), autotune_trial=512, tuning=tuning)
     torch.cuda.synchronize()
+    warm_s = time.perf_counter() - t0
     times = []
-    for _ in range(args.steps):
+    for _ in range(steps):
         jobs = mk()
         t0 = time.perf_counter()
-        scan_queue(jobs, autotune_trial=0)
+        scan_queue(jobs, tuning=tuning)
         torch.cuda.synchronize()
         times.append(time.perf_counter() - t0)
     total_rot = rot.shape[0] * len(cases)
-    value = total_rot * len(times) / sum(times)
-    # the same queue captured once into one CUDA graph, replayed (setup outside the timing)
-    from powerfit_gb300.queue import QueueGraph
-    qg = QueueGraph(mk(), autotune_trial=0)
-    for _ in range(max(1, args.warmup)):
+    qg = QueueGraph(mk(), tuning=tuning)
+    for _ in range(max(1, warmup)):
         qg.replay()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         qg.replay()
     torch.cuda.synchronize()
     graph_s = time.perf_counter() - t0
     qg.close()
-    line = {"metric": "map-rotations/s, queue of 16 uneven maps (1 GB300)", "value": value,
-            "unit": "map-rotations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 FFT / float-float LCC", "data": "synthetic (%s)" % desc,
-            "config": {"workload": "queue16", "grids": [c.target.shape[0] for c in cases],
-                       "rotations_per_map": int(rot.shape[0]), "rotations_per_batch": 256,
-                       "timing": "host wall clock per step: per-map setup (spectra, template) + all scans"},
-            "graph": {"value": total_rot * args.steps / graph_s, "unit": "map-rotations/s",
-                      "ms_per_replay": 1e3 * graph_s / args.steps,
+    return {"metric": "map-rotations/s, queue of 16 uneven maps (1 GB300)",
+            "value": total_rot * len(times) / sum(times), "unit": "map-rotations/s", "steps": steps,
+            "ms_per_step": 1e3 * sum(times) / len(times), "data": "synthetic (%s)" % desc,
+            "grids": [c.target.shape[0] for c in cases], "rotations_per_map": int(rot.shape[0]),
+            "tuning": {"x".join(str(v) for v in k): {kk: vv for kk, vv in t.items() if kk != "trial_ms"}
+                       for k, t in tuning.items()},
+            "tuning_source": "autotuner (512-rotation trials), once per grid size in the warm-up (%.1f s)" % warm_s,
+            "timing": "host wall clock per step: per-map setup (spectra, template, rotations) + all scans",
+            "graph": {"value": total_rot * steps / graph_s, "unit": "map-rotations/s",
+                      "ms_per_replay": 1e3 * graph_s / steps,
                       "timing": "one CUDA graph of all 16 maps' scans (captured once), host wall clock per replay"}}
+
+
+def run_queue(args):
+    """The uneven-map queue on its own line (``--config queue16``)."""
+    q = queue_leg(args.steps, args.warmup, args.rotations)
+    line = {"metric": q["metric"], "value": q["value"], "unit": q["unit"], "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": q["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 FFT / float-float LCC", "data": q["data"],
+            "config": {"workload": "queue16", "grids": q["grids"], "rotations_per_map": q["rotations_per_map"],
+                       "tuning": q["tuning"], "tuning_source": q["tuning_source"], "timing": q["timing"]},
+            "graph": q["graph"]}
     print(json.dumps(line), flush=True)
     return 0
 

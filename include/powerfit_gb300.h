@@ -131,19 +131,22 @@ int pf_fft3d(pf_ctx *ctx, const float *in, float *out);
  * normalised and filtered, N float32), lcc mask (N uint8), template and mask
  * (N float32 each, after the mask setter's preprocessing), rotations (nrot x 9
  * float64, row-major); outputs lcc (N float32) and rot (N int32), zeroed by
- * the call.  Results equal pf_scan's for the same inputs.  The target
- * spectra, one rotation pair's intermediate spectra, the twiddle tables and
- * the converted rotations live in one file-scope device array of about
- * 10.1 MiB (grids up to 64^3 voxels, edges <= 256, (z, y) plane within shared
- * memory); larger grids return PF_E_SHAPE.  Every GPU that loads the library
- * holds that array until the process exits.
+ * the call.  Results equal pf_scan's for the same inputs within float32
+ * rounding.  The target spectra, one rotation pair's intermediate spectra,
+ * the twiddle tables (built on the device by the call) and the converted
+ * rotations live in one file-scope device array of about 10.1 MiB (grids up
+ * to 64^3 voxels, edges <= 256, (z, y) plane within shared memory); larger
+ * grids return PF_E_SHAPE.  Every GPU that loads the library holds that array
+ * until the process exits.
  *
- * The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress), with that device current; make that first call
- * before any stream capture.  Work is queued on `stream` and the call returns
- * without waiting.  All calls share the one array: calls that overlap on the
- * GPU (different streams, or a second call before the first has finished on
- * another stream) race and corrupt each other's results. */
+ * The first call on each device does a one-time set-up with that device
+ * current: it looks up the array's device address (cudaGetSymbolAddress) and
+ * sets the kernels' shared-memory limits.  Make that first call before any
+ * stream capture.  Every call queues its work on `stream` and returns
+ * without waiting for it.  All calls share the one array and it keeps the
+ * last call's contents (each call rebuilds what it reads): calls that overlap
+ * on the GPU (different streams, or a second call before the first has
+ * finished on another stream) race and corrupt each other's results. */
 int pf_scan_noalloc(int nz, int ny, int nx, const float *d_target, const uint8_t *d_lcc_mask,
                     const float *d_template, const float *d_mask, double norm_factor, int rmax,
                     const double *d_rotmats, int64_t nrot, int64_t rot_offset,

@@ -4,10 +4,12 @@
 ``oracle/liboracle_rotate.so`` (plain gcc, works on x86-64 and aarch64).
 
 ``build_ref()`` compiles the reference's own native sources where they lie
-(``/root/reference/src/powerfit_em/_extensions.c`` and ``_powerfit.pyx``) into
-``oracle/_ref/``, with the flags of the reference's ``setup.py:11-25``
-(``-ffast-math`` for ``_extensions.c``).  It runs only where the reference
-tree and Cython are present; nothing is copied out of the reference tree.
+(``src/powerfit_em/_extensions.c`` and ``_powerfit.pyx`` of the reference
+checkout named by ``$POWERFIT_REFERENCE_ROOT``, by default the build
+container's checkout) into ``oracle/_ref/``, with the flags of the
+reference's ``setup.py:11-25`` (``-ffast-math`` for ``_extensions.c``).  It
+runs only where the reference tree and Cython are present; nothing is copied
+out of the reference tree.
 """
 from __future__ import annotations
 
@@ -18,7 +20,8 @@ import sys
 import sysconfig
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = "/root/reference/src/powerfit_em"
+REF_ROOT = os.environ.get("POWERFIT_REFERENCE_ROOT", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "src", "powerfit_em")
 REF_OUT = os.path.join(HERE, "_ref")
 
 

@@ -203,6 +203,34 @@ def _worker(args):
     return scan(p, rotations)
 
 
+def _timed_worker(args):
+    """``_worker`` with its two phases timed: the correlator's set-up
+    (``prepare``: Laplace filter and target spectra) and the rotation loop."""
+    import time
+    target, template, mask, laplace_filter, rotations = args
+    t0 = time.perf_counter()
+    p = prepare(target, template, mask, laplace_filter)
+    t1 = time.perf_counter()
+    lcc, rot = scan(p, rotations)
+    return lcc, rot, t1 - t0, time.perf_counter() - t1, rotations.shape[0]
+
+
+def cpu_scan_timed(target, template, mask, rotations, laplace_filter=False, nproc=1, pool=None):
+    """``cpu_scan`` (same slices and merge) that also returns, per process, the
+    set-up seconds, the rotation-loop seconds and the rotations it scanned:
+    (lcc, rot, [(prepare_s, scan_s, nrot), ...])."""
+    rotations = np.asarray(rotations, dtype=np.float64).reshape(-1, 3, 3)
+    nrot = rotations.shape[0]
+    per = nrot // nproc
+    jobs = []
+    for n in range(nproc):
+        end = None if n == nproc - 1 else (n + 1) * per
+        jobs.append((target, template, mask, laplace_filter, rotations[n * per:end]))
+    res = [_timed_worker(jobs[0])] if (pool is None and nproc == 1) else pool.map(_timed_worker, jobs)
+    lcc, rot = combine([(r[0], r[1]) for r in res], per)
+    return lcc, rot, [(r[2], r[3], r[4]) for r in res]
+
+
 def cpu_scan(target, template, mask, rotations, laplace_filter=False, nproc=1, pool=None):
     """Restates ``PowerFitter._cpu_scan``: contiguous rotation slices per process,
     then ``_combine``.  ``pool`` is a ``multiprocessing`` pool started with
@@ -219,3 +247,50 @@ def cpu_scan(target, template, mask, rotations, laplace_filter=False, nproc=1, p
     else:
         parts = pool.map(_worker, jobs)
     return combine(parts, per)
+
+
+# ---------------------------------------------------------------------------
+# Top-two scan over contiguous rotation slices on several processes (parity
+# checks of the large grids): each slice is ``scan(track_second=True)``; the
+# slices merge in rotation order with the strict ``>`` of ``scan`` (lower index
+# wins ties), the runner-up of a voxel being the larger of the loser's best and
+# the winner's own runner-up.
+# ---------------------------------------------------------------------------
+
+def _top2_worker(job):
+    target, template, mask, laplace_filter, rots = job
+    p = prepare(target, template, mask, laplace_filter)
+    return scan(p, rots, track_second=True)
+
+
+def merge_top2(parts, offsets):
+    """Merge per-slice (lcc, rot, second) in slice order; ``offsets[k]`` is the
+    first rotation index of slice k."""
+    lcc = np.zeros(parts[0][0].shape)
+    rot = np.zeros(parts[0][0].shape)
+    second = np.zeros(parts[0][0].shape)
+    for (pl, pr, ps), off in zip(parts, offsets):
+        better = pl > lcc
+        second = np.where(better, np.maximum(lcc, ps), np.maximum(second, np.where(pl > second, pl, second)))
+        lcc = np.where(better, pl, lcc)
+        rot = np.where(better, pr + off, rot)
+    return lcc, rot, second
+
+
+def scan_top2_parallel(target, template, mask, rotations, laplace_filter=False, nproc=None):
+    """``scan(track_second=True)`` of the prepared inputs over ``rotations``,
+    split into contiguous slices on a ``spawn`` pool of ``nproc`` processes
+    (safe after CUDA initialisation in the parent)."""
+    import multiprocessing as mp
+    rotations = np.asarray(rotations, dtype=np.float64).reshape(-1, 3, 3)
+    nrot = rotations.shape[0]
+    nproc = max(1, min(nproc or os.cpu_count() or 1, nrot))
+    per = -(-nrot // nproc)
+    offsets = list(range(0, nrot, per))
+    jobs = [(target, template, mask, laplace_filter, rotations[o:o + per]) for o in offsets]
+    if len(jobs) == 1:
+        parts = [_top2_worker(jobs[0])]
+    else:
+        with mp.get_context("spawn").Pool(len(jobs)) as pool:
+            parts = pool.map(_top2_worker, jobs)
+    return merge_top2(parts, offsets)

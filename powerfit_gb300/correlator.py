@@ -129,12 +129,52 @@ class CUDACorrelator(BaseCorrelator):
         self._ctx.set_template_mask(self._template, self._mask, float(self._norm_factor), self._rmax)
 
     def scan(self, rot_offset=0):
+        self._start(rot_offset)
+        while self._launch_next():
+            self._wait()
+        self._results()
+
+    # The scan in steps, so that several devices run at once (PowerFitter.scan
+    # launches the same step on every device before waiting on any).  Without
+    # a progress counter the whole set is one asynchronous call.  With one
+    # (the reference advances it once per rotation, powerfitter.py:332-333, and
+    # its driver polls it, :120-128), the set runs in slices of whole rotation
+    # batches, about a hundredth of the set each, and the counter advances as
+    # each slice completes; slices of whole batches accumulate to the same
+    # results as one call, bit for bit.
+    def _start(self, rot_offset=0):
         super().scan()
-        self._lcc, self._rot = self._ctx.scan(self._rotations, rot_offset=rot_offset, flags=self._flags)
+        self._rot_offset = int(rot_offset)
+        self._ctx.set_rotations(self._rotations)
+        nrot = self._rotations.shape[0]
+        step = nrot
+        if getattr(self, "_counter", None) is not None:
+            pairs, _, _ = self._ctx.get_tuning()
+            batch = 2 * max(1, pairs)
+            step = batch * max(1, -(-nrot // (100 * batch)))
+        self._slices = [(f, min(step, nrot - f)) for f in range(0, nrot, max(step, 1))] or [(0, 0)]
+        self._next = 0
+
+    def _launch_next(self):
+        """Queue the next slice (asynchronous); False when none is left."""
+        if self._next >= len(self._slices):
+            return False
+        first, count = self._slices[self._next]
+        self._ctx.scan_resident(first, count, self._rot_offset,
+                                self._flags | (_lib.PF_FLAG_ACCUMULATE if self._next else 0))
+        return True
+
+    def _wait(self):
+        """Wait for the slice in flight and advance the progress counter."""
+        self._ctx.synchronize()
         counter = getattr(self, "_counter", None)
         if counter is not None:
-            for _ in range(self._rotations.shape[0]):
+            for _ in range(self._slices[self._next][1]):
                 counter.increment()
+        self._next += 1
+
+    def _results(self):
+        self._lcc, self._rot = self._ctx.get_results()
 
     @property
     def context(self):
@@ -203,7 +243,7 @@ class PowerFitter:
         rot = np.asarray(self._rotations, dtype=np.float64).reshape(-1, 3, 3)
         nrot = rot.shape[0]
         per = nrot // len(devices)
-        parts = []
+        corrs = []
         for n, dev in enumerate(devices):
             end = None if n == len(devices) - 1 else (n + 1) * per
             corr = CUDACorrelator(self._array(self._target), laplace=self._laplace, device=dev,
@@ -211,9 +251,22 @@ class PowerFitter:
             corr.template = self._array(self._template)
             corr.mask = self._array(self._mask)
             corr.rotations = rot[n * per:end]
-            corr.scan()
+            corrs.append(corr)
+        # every device's slice is queued before any is waited on: the devices
+        # search their rotations at the same time
+        for corr in corrs:
+            corr._start()
+        while True:
+            running = [corr for corr in corrs if corr._launch_next()]
+            if not running:
+                break
+            for corr in running:
+                corr._wait()
+        parts = []
+        for corr in corrs:
+            corr._results()
             parts.append((corr.lcc, corr.rot))
-            self._corr = corr
+        self._corr = corrs[-1]
         if len(parts) == 1:
             self._lcc, self._rot = parts[0]
         else:

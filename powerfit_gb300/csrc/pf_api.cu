@@ -1156,23 +1156,53 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 constexpr int kNoAllocMaxDevices = 64;
 unsigned char* g_noalloc_addr[kNoAllocMaxDevices] = {};
+size_t g_noalloc_smem[kNoAllocMaxDevices] = {};
 std::mutex g_noalloc_mutex;
 
-// device address of the scratch on the current device (set up on first use)
-int noalloc_scratch(unsigned char** out) {
+// One-time set-up per device, with that device current: the scratch's device
+// address (cudaGetSymbolAddress), the largest shared memory a block may opt
+// in to, and the kernels' dynamic shared-memory limits.  Later calls on the
+// device only read what this stored.
+int noalloc_setup(unsigned char** out, size_t* smem_optin) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
     return fail(nullptr, PF_E_CUDA, "pf_scan_noalloc: no current CUDA device");
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
   if (!g_noalloc_addr[dev]) {
+    int optin = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess || optin <= 0)
+      return fail(nullptr, PF_E_CUDA, "pf_scan_noalloc: no shared-memory limit for device %d: %s", dev,
+                  cudaGetErrorString(e));
+    const size_t m = (size_t)optin;
+    if ((e = allow_smem(k_pass1<false>, m)) != cudaSuccess || (e = allow_smem(k_pass2<false>, m)) != cudaSuccess ||
+        (e = allow_smem(k_pass3<false>, m)) != cudaSuccess || (e = allow_smem(k_fwd_x_real, m)) != cudaSuccess)
+      return fail(nullptr, PF_E_CUDA, "pf_scan_noalloc: kernel attributes: %s", cudaGetErrorString(e));
     void* ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess || !ptr)
       return fail(nullptr, PF_E_CUDA, "pf_scan_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+    g_noalloc_smem[dev] = m;
     g_noalloc_addr[dev] = (unsigned char*)ptr;
   }
   *out = g_noalloc_addr[dev];
+  *smem_optin = g_noalloc_smem[dev];
   return PF_OK;
+}
+
+// The twiddle tables of the three edges, built on the device: table a (x, y,
+// z) at tw + a * kNoAllocMaxEdge holds exp(-2 pi i m / n_a), m < n_a, the same
+// values the contexts upload (cos and sin of the angle in float64, rounded to
+// float32; sincospi takes the angle as a multiple of pi).
+__global__ void k_noalloc_twiddles(float2* __restrict__ tw, int nx, int ny, int nz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * kNoAllocMaxEdge) return;
+  const int a = i / kNoAllocMaxEdge, m = i - a * kNoAllocMaxEdge;
+  const int n = a == 0 ? nx : (a == 1 ? ny : nz);
+  if (m >= n) return;
+  double sn, cs;
+  sincospi(2.0 * (double)m / (double)n, &sn, &cs);
+  tw[i] = make_float2((float)cs, (float)-sn);
 }
 
 __global__ void k_rot_to_fixed(const double* __restrict__ rd, long long n, RotFixed* __restrict__ out) {
@@ -1216,15 +1246,12 @@ int pf_scan_noalloc(int nz, int ny, int nx, const float* d_target, const uint8_t
   AxisPlan px, py, pz;
   if (!plan_of(nx, &px) || !plan_of(ny, &py) || !plan_of(nz, &pz))
     return fail(nullptr, PF_E_SHAPE, "pf_scan_noalloc: every edge must factor into 2, 3, 5 and 7");
-  int dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceProp prop;
-  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return fail(nullptr, PF_E_CUDA, "no device properties");
-  if (plane_smem(ny, nz) > prop.sharedMemPerBlockOptin)
-    return fail(nullptr, PF_E_SHAPE, "pf_scan_noalloc: the (z, y) plane does not fit in shared memory");
   unsigned char* scratch = nullptr;
-  int rc = noalloc_scratch(&scratch);
+  size_t smem_optin = 0;
+  int rc = noalloc_setup(&scratch, &smem_optin);
   if (rc) return rc;
+  if (plane_smem(ny, nz) > smem_optin)
+    return fail(nullptr, PF_E_SHAPE, "pf_scan_noalloc: the (z, y) plane does not fit in shared memory");
   cudaStream_t s = (cudaStream_t)stream;
   const long long N = (long long)nz * ny * nx;
   float2* spec = (float2*)scratch;
@@ -1234,23 +1261,9 @@ int pf_scan_noalloc(int nz, int ny, int nx, const float* d_target, const uint8_t
   float2* twz = twy + kNoAllocMaxEdge;
   RotFixed* rots = (RotFixed*)(scratch + kNoAllocSpecBytes + kNoAllocBufBytes + kNoAllocTwBytes);
 
-  // kernel attributes (idempotent) and twiddles (host tables, as for contexts)
-  const size_t m = prop.sharedMemPerBlockOptin;
-  PF_CUDA(nullptr, allow_smem(k_pass1<false>, m));
-  PF_CUDA(nullptr, allow_smem(k_pass2<false>, m));
-  PF_CUDA(nullptr, allow_smem(k_pass3<false>, m));
-  PF_CUDA(nullptr, allow_smem(k_fwd_x_real, m));
-  float2 tw_host[3][kNoAllocMaxEdge];   // same tables as the contexts build (twiddles())
-  const int edges[3] = {nx, ny, nz};
-  for (int a = 0; a < 3; ++a)
-    for (int mm = 0; mm < edges[a]; ++mm) {
-      const double ang = 2.0 * M_PI * (double)mm / (double)edges[a];
-      tw_host[a][mm] = make_float2((float)std::cos(ang), (float)-std::sin(ang));
-    }
-  // pageable source: the copies are staged before the calls return
-  PF_CUDA(nullptr, cudaMemcpyAsync(twx, tw_host[0], nx * sizeof(float2), cudaMemcpyHostToDevice, s));
-  PF_CUDA(nullptr, cudaMemcpyAsync(twy, tw_host[1], ny * sizeof(float2), cudaMemcpyHostToDevice, s));
-  PF_CUDA(nullptr, cudaMemcpyAsync(twz, tw_host[2], nz * sizeof(float2), cudaMemcpyHostToDevice, s));
+  // twiddle tables, built on the device
+  k_noalloc_twiddles<<<(3 * kNoAllocMaxEdge + 255) / 256, 256, 0, s>>>(twx, nx, ny, nz);
+  PF_CUDA(nullptr, cudaGetLastError());
 
   // target spectra FT(target)/N and FT(target^2)/N into the scratch
   Geometry g{};

@@ -20,6 +20,21 @@ def rotation_shard(nrot, rank, world):
     return start, stop
 
 
+def weak_scaling_shard(rotations_for, nset, rank, world):
+    """Rotations of `rank` when every rank scans `nset` rotations of its own
+    (weak scaling): one set of ``world * nset`` rotations (``rotations_for(count)``
+    builds a set of that size) split into contiguous shards, so that no two
+    ranks scan the same rotation and every stored index is a global index of
+    that set.  Returns (the rank's (nset, 3, 3) rotations, the global index of
+    its first rotation); scanning with that index as the rotation offset makes
+    the merged indices lie in [0, world * nset)."""
+    if world <= 1:
+        return rotations_for(nset), 0
+    full = rotations_for(world * nset)
+    start, stop = rotation_shard(world * nset, rank, world)
+    return full[start:stop], start
+
+
 def merge_parts(parts, offsets, merge_one=None):
     """Merge [(lcc, rot), ...] in shard order; shard n's indices get offsets[n].
 

@@ -7,6 +7,13 @@ kernels for its grid) on its own CUDA stream; after the per-map setup
 is awaited, so the kernels of small maps run beside those of large ones and
 fill the GPU together.  Results equal per-map scans (same kernels, same
 order of rotations per voxel).
+
+Batch and tile shapes: a job's ``pairs`` fixes the rotation pairs per batch;
+with ``pairs = 0`` the library's autotuner (``pf_autotune``) picks pairs per
+batch and the tile rows of passes 1 and 3 from short timed trial scans.  A
+``tuning`` dict shared across calls keeps the choice per grid shape, so a
+queue autotunes each size it holds once and reuses the shapes for every later
+map of that size.
 """
 from __future__ import annotations
 
@@ -40,11 +47,27 @@ class MapJob:
     rot: np.ndarray = field(default=None, repr=False)
 
 
-def scan_queue(jobs, device=0, autotune_trial=256, streams=None):
+def _tune(ctx, job, nrot, autotune_trial, tuning):
+    """Batch and tile shapes of one map: the job's fixed pairs, the shapes
+    already chosen for its grid shape in ``tuning``, or the autotuner's."""
+    if job.pairs:
+        ctx.set_tuning(pairs=job.pairs)
+        return
+    key = tuple(job.target.shape)
+    if tuning is not None and key in tuning:
+        ctx.set_tuning(**{k: tuning[key][k] for k in ("pairs", "rows1", "rows3")})
+    elif autotune_trial:
+        cfg = ctx.autotune(min(autotune_trial, nrot))
+        if tuning is not None:
+            tuning[key] = cfg
+
+
+def scan_queue(jobs, device=0, autotune_trial=256, streams=None, tuning=None):
     """Scan every job; fills ``job.lcc`` / ``job.rot`` and returns the jobs.
 
     ``streams``: torch CUDA streams or raw ``cudaStream_t`` handles, one per
-    job (default: a new torch stream per job).
+    job (default: a new torch stream per job).  ``tuning``: a dict of batch and
+    tile shapes per grid shape, read and filled (see the module docstring).
     """
     import torch
     torch.cuda.set_device(device)
@@ -62,10 +85,7 @@ def scan_queue(jobs, device=0, autotune_trial=256, streams=None):
         ctx.set_target(ftarget, base._lcc_mask)
         ctx.set_template_mask(base._template, base._mask, float(base._norm_factor), base._rmax)
         nrot = ctx.set_rotations(job.rotations)
-        if job.pairs:
-            ctx.set_tuning(pairs=job.pairs)
-        elif autotune_trial:
-            ctx.autotune(min(autotune_trial, nrot))
+        _tune(ctx, job, nrot, autotune_trial, tuning)
         contexts.append((ctx, nrot))
     # queue every scan before waiting for any
     for job, (ctx, nrot) in zip(jobs, contexts):
@@ -89,7 +109,7 @@ class QueueGraph:
     results from scratch.
     """
 
-    def __init__(self, jobs, device=0, autotune_trial=256):
+    def __init__(self, jobs, device=0, autotune_trial=256, tuning=None):
         import torch
         torch.cuda.set_device(device)
         self.device = device
@@ -106,10 +126,7 @@ class QueueGraph:
             ctx.set_target(ftarget, base._lcc_mask)
             ctx.set_template_mask(base._template, base._mask, float(base._norm_factor), base._rmax)
             nrot = ctx.set_rotations(job.rotations)
-            if job.pairs:
-                ctx.set_tuning(pairs=job.pairs)
-            elif autotune_trial:
-                ctx.autotune(min(autotune_trial, nrot))
+            _tune(ctx, job, nrot, autotune_trial, tuning)
             self.contexts.append((ctx, nrot))
         self._scan_all()                        # warm-up: allocates every buffer the scans use
         torch.cuda.synchronize(device)

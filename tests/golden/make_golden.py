@@ -1,7 +1,9 @@
-"""Generate the golden fixtures from the real reference (run in a container that
-has the reference tree at /root/reference; the fixtures are committed).
+"""Generate the golden fixtures from the real reference (run where the reference
+checkout is present, ``$POWERFIT_REFERENCE_ROOT`` as in ``oracle/build.py``; the
+fixtures are committed).
 
-    python tests/golden/make_golden.py [prep]   (``prep``: only prep.npz, ref_map.mrc, analyzer.npz)
+    python tests/golden/make_golden.py [prep|rotset]
+        (``prep``: only prep.npz, ref_map.mrc, analyzer.npz; ``rotset``: those and rotset_471.npz)
 
 Each fixture records reference outputs for seeded inputs:
 
@@ -14,6 +16,10 @@ Each fixture records reference outputs for seeded inputs:
   ``helpers.determine_core_indices`` on seeded inputs.
 * ``ref_map.mrc``: a map written by the reference's ``volume.to_mrc``;
   ``analyzer.npz``: the reference ``Analyzer``'s solutions on seeded peaks.
+* ``rotset_471.npz``: a strided 2,048-row slice of the reference's 4.71 degree
+  orientation set (``c48u2947.npy`` through ``rotations.proportional_orientations``),
+  its quaternions, weights and the reference's ``quat_to_rotmat`` of them: the
+  128^3 parity tests scan the reference's own rotations.
 * ``scan_<name>.npz``: ``CPUCorrelator`` (numpy.fft path) full scans:
   inputs (float32-exact), rotations, best LCC, best rotation and, from the
   oracle restatement (checked equal to the reference first), the per-voxel
@@ -187,6 +193,15 @@ def gen_scan(powerfitter, helpers, name, target, template, mask, rotmats, laplac
     print(name, "max lcc %.4f" % np.nanmax(lcc), "oracle err %.2e" % err)
 
 
+def gen_rotset(rot):
+    """A strided slice (every 34th row, 2,048 rows) of the 4.71 degree set."""
+    q, w, degree = rot.proportional_orientations(4.71)
+    rows = np.arange(0, q.shape[0], 34)[:2048]
+    np.savez_compressed(os.path.join(HERE, "rotset_471.npz"), rows=rows, quat=q[rows], weights=w[rows],
+                        rotmats=rot.quat_to_rotmat(q[rows]), degree=degree, set_size=q.shape[0])
+    print("rotset_471", rows.shape[0], "rows of", q.shape[0], degree)
+
+
 def main():
     if refimport.load() is None:
         raise SystemExit("reference tree not available")
@@ -198,6 +213,9 @@ def main():
     gen_prep(pfx, powerfitter, helpers)
     gen_io(refimport.module("volume"), refimport.module("analyzer"))
     if len(sys.argv) > 1 and sys.argv[1] == "prep":
+        return
+    gen_rotset(rot)
+    if len(sys.argv) > 1 and sys.argv[1] == "rotset":
         return
     gen_rotate(ext, rot)
     gen_helpers(pfx)

@@ -40,17 +40,31 @@ def _case():
     return p, rot
 
 
-def _rank_main(rank, world, port, q):
+def _weak_set(count):
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    return quat_to_rotmat(super_fibonacci(count))
+
+
+def _rank_main(rank, world, port, q, weak=False):
     import torch.distributed as dist
     from oracle import oracle as O
-    from powerfit_gb300.distributed import gather_and_merge
+    from powerfit_gb300.distributed import gather_and_merge, weak_scaling_shard
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
         p, rot = _case()
-        a, b = rotation_shard(rot.shape[0], rank, world)
-        lcc, r = O.scan(p, rot[a:b])
-        out = gather_and_merge(lcc.astype(np.float32), r.astype(np.int32), a, merge_one=_oracle_merge_one)
+        if weak:
+            # the bench's multi-rank form: every rank scans 5 rotations of its
+            # own, stored with global indices (the rotation offset), merged
+            # without a rank offset
+            mine, first = weak_scaling_shard(_weak_set, 5, rank, world)
+            lcc, r = O.scan(p, mine)
+            out = gather_and_merge(lcc.astype(np.float32), (r + first).astype(np.int32), 0,
+                                   merge_one=_oracle_merge_one)
+        else:
+            a, b = rotation_shard(rot.shape[0], rank, world)
+            lcc, r = O.scan(p, rot[a:b])
+            out = gather_and_merge(lcc.astype(np.float32), r.astype(np.int32), a, merge_one=_oracle_merge_one)
         if rank == 0:
             q.put((out[0], out[1]))
         else:
@@ -73,14 +87,12 @@ def test_merge_ties_keep_lower_shard():
     assert np.array_equal(rot, [1, 11]) and np.array_equal(lcc, np.array([0.5, 0.3], np.float32))
 
 
-def test_two_gloo_ranks_equal_single_scan():
+def _run_ranks(weak):
     import multiprocessing as mp
-    pytest.importorskip("torch")
-    from oracle import oracle as O
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q, weak)) for r in range(2)]
     for pr in procs:
         pr.start()
     results = [q.get(timeout=120) for _ in procs]
@@ -89,9 +101,34 @@ def test_two_gloo_ranks_equal_single_scan():
         assert pr.exitcode == 0
     merged = [r for r in results if r is not None]
     assert len(merged) == 1
-    lcc, rot = merged[0]
+    return merged[0]
+
+
+def test_two_gloo_ranks_equal_single_scan():
+    pytest.importorskip("torch")
+    from oracle import oracle as O
+    lcc, rot = _run_ranks(False)
     p, rots = _case()
     rl, rr = O.scan(p, rots)
     assert np.allclose(lcc, rl.astype(np.float32))
     upd = rl > 0
     assert np.array_equal(rot[upd], rr[upd].astype(np.int32))
+
+
+def test_weak_scaling_shards_merge_to_global_indices():
+    """Two ranks, each scanning a shard of its own (the bench's torchrun
+    form): the merged volumes equal one scan over the two ranks' whole set,
+    and every merged index lies inside that set."""
+    pytest.importorskip("torch")
+    from oracle import oracle as O
+    from powerfit_gb300.distributed import weak_scaling_shard
+    a, fa = weak_scaling_shard(_weak_set, 5, 0, 2)
+    b, fb = weak_scaling_shard(_weak_set, 5, 1, 2)
+    assert (fa, fb) == (0, 5) and np.array_equal(np.concatenate([a, b]), _weak_set(10))
+    lcc, rot = _run_ranks(True)
+    p, _ = _case()
+    rl, rr = O.scan(p, _weak_set(10))
+    assert np.allclose(lcc, rl.astype(np.float32))
+    upd = rl > 0
+    assert np.array_equal(rot[upd], rr[upd].astype(np.int32))
+    assert rot.min() >= 0 and rot.max() < 10

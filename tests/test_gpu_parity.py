@@ -325,3 +325,65 @@ def test_map_queue_equals_single_scans():
     for job in jobs:
         ref = correlator(job.target, job.template, job.mask, rot, job.laplace)
         assert np.array_equal(job.lcc, ref.lcc) and np.array_equal(job.rot, ref.rot)
+
+
+def test_queue16_autotuned_equals_single_scans():
+    """The uneven-map queue of the benchmark (16 seeded maps, 48^3-160^3),
+    every map's scan on its own stream with autotuned batch and tile shapes
+    (tuned once per grid size), equals a single scan of each map, bit for bit;
+    so does one replay of the same queue captured as a CUDA graph."""
+    from powerfit_gb300.queue import MapJob, QueueGraph, make_queue, scan_queue
+    from powerfit_gb300.rotations import rotation_set
+    rot, _ = rotation_set(10.0, data_dir="/nonexistent")
+    rot = rot[::100]                                       # 75 rotations of the 9.72 degree set's size
+    cases = make_queue(16, seed=0)
+    mk = lambda: [MapJob(c.target.astype(np.float64), c.template, c.mask, rot) for c in cases]
+    tuning = {}
+    jobs = scan_queue(mk(), autotune_trial=64, tuning=tuning)
+    assert sorted(tuning) == sorted({tuple(c.target.shape) for c in cases})
+    qg = QueueGraph(mk(), tuning=tuning)
+    qg.replay()
+    gjobs = qg.results()
+    for job, gjob in zip(jobs, gjobs):
+        ref = correlator(job.target, job.template, job.mask, rot, job.laplace)
+        assert np.array_equal(job.lcc, ref.lcc) and np.array_equal(job.rot, ref.rot), job.target.shape
+        assert np.array_equal(gjob.lcc, ref.lcc) and np.array_equal(gjob.rot, ref.rot), job.target.shape
+    qg.close()
+
+
+def test_progress_counter_and_concurrent_devices():
+    """The progress counter advances while the scan runs, one slice of whole
+    batches at a time (the reference increments it per rotation and polls
+    it, powerfitter.py:120-128, 332-333), with results equal to one call; and
+    PowerFitter over two device slots (both device 0 here) launches every
+    slot's slice before waiting on any and merges them to the single scan."""
+    from powerfit_gb300 import CUDACorrelator
+    from powerfit_gb300.correlator import PowerFitter
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    target, template, mask = _synthetic((48, 48, 48), 2.5, 800, 8.0, 9, False)
+    rot = quat_to_rotmat(super_fibonacci(40))    # 20 per device slot: the same rotation pairs as one scan
+    base = correlator(target, template, mask, rot, False)
+
+    class Counter:
+        n = 0
+
+        def increment(self):
+            self.n += 1
+
+    corr = CUDACorrelator(target)
+    corr.context.set_tuning(pairs=2)             # batches of 4 rotations: 10 slices
+    corr.template = template
+    corr.mask = mask
+    corr.rotations = rot
+    corr._counter = Counter()
+    seen = []
+    sync = corr.context.synchronize
+    corr.context.synchronize = lambda: (seen.append(corr._counter.n), sync())
+    corr.scan()
+    assert corr._counter.n == 40 and seen == list(range(0, 40, 4))
+    assert np.array_equal(corr.lcc, base.lcc) and np.array_equal(corr.rot, base.rot)
+
+    pf = PowerFitter(target)
+    pf._template, pf._mask, pf._rotations, pf._devices = template, mask, rot, [0, 0]
+    pf.scan()
+    assert np.array_equal(pf._lcc, base.lcc) and np.array_equal(pf._rot, base.rot)

@@ -1,0 +1,88 @@
+"""GPU parity on the large grids, against the float64 oracle run live.
+
+The compile-time kernels of every large fast size are compared directly with
+the oracle restatement of ``CPUCorrelator.scan`` (``powerfitter.py:317-393``):
+
+* 128^3, the filtered workload (1.5 A/voxel, 6 copies of a 4,000-atom chain at
+  6 A, SNR 3, Laplace + core-weighted), on 32 rotations of the reference's own
+  4.71 degree set (``tests/golden/rotset_471.npz``, written by
+  ``make_golden.py`` from ``c48u2947.npy``);
+* 192^3, the precision-study workload (1.2 A/voxel, 8 copies of a 10,000-atom
+  chain at 4.5 A, SNR 2), through the four-block clustered plane pass;
+* 160^3 and 96^3, maps of the uneven queue's sizes (one block a plane).
+
+Criterion (as every parity test here): best LCC within 1e-4 absolute; best
+rotation identical wherever the oracle's top-two gap exceeds 1e-4.  The oracle
+runs on contiguous rotation slices in a spawn-started process pool.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+LCC_TOL = 1e-4
+GAP_TOL = 1e-4
+
+
+def _parity(target, template, mask, rot, laplace, label):
+    from powerfit_gb300 import CUDACorrelator
+    corr = CUDACorrelator(target, laplace=laplace)
+    corr.template = template
+    corr.mask = mask
+    corr.rotations = rot
+    corr.scan()
+    ref, ref_rot, second = O.scan_top2_parallel(target, template, mask, rot, laplace)
+    fin = np.isfinite(ref)
+    assert np.array_equal(np.isfinite(corr.lcc), fin), label
+    err = float(np.max(np.abs(corr.lcc[fin] - ref[fin])))
+    clear = fin & ((ref - second) > GAP_TOL)
+    bad = int(np.sum(corr.rot[clear] != ref_rot[clear]))
+    hit = int(np.sum(ref > 0))
+    print("%s: max|dLCC| %.2e over %d voxels, argmax identical on %d clear voxels (%d differ)"
+          % (label, err, int(fin.sum()), int(clear.sum()), bad))
+    assert err < LCC_TOL, "%s: max |dLCC| = %g" % (label, err)
+    assert bad == 0, "%s: %d of %d clear voxels pick a different rotation" % (label, bad, int(clear.sum()))
+    assert clear.sum() > 0.5 * hit, "%s: too few voxels with a clear best rotation" % label
+    return corr
+
+
+def _config(name, seed=0):
+    from powerfit_gb300 import synth
+    from powerfit_gb300.correlator import determine_core_indices
+    cfg = synth.CONFIGS[name]
+    case = synth.make_config(name, seed=seed)
+    mask = determine_core_indices(case.mask) if cfg["core_weighted"] else case.mask
+    return cfg, case.target.astype(np.float64), case.template, mask
+
+
+def test_scan_oracle_128_reference_rotations():
+    d = np.load(os.path.join(GOLD, "rotset_471.npz"))
+    rot = d["rotmats"][::64]                       # 32 rotations spread over the 4.71 degree set
+    assert rot.shape[0] == 32
+    cfg, target, template, mask = _config("lcc128_filtered")
+    corr = _parity(target, template, mask, rot, cfg["laplace"], "128^3 Laplace + core-weighted")
+    geo = corr.context.get_geometry()
+    assert geo["valid_planes"] < 128               # the pruned fast path ran
+
+
+def test_scan_oracle_192_clustered_plane_pass():
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    cfg, target, template, mask = _config("lcc192_precision")
+    rot = quat_to_rotmat(super_fibonacci(70728))[::11788]   # 6 rotations of a set of the 4.71 degree size
+    _parity(target, template, mask, rot, cfg["laplace"], "192^3 (clustered plane pass)")
+
+
+@pytest.mark.parametrize("n,vs,natoms,laplace", [(160, 1.3, 5000, True), (96, 2.0, 2500, False)])
+def test_scan_oracle_queue_sizes(n, vs, natoms, laplace):
+    from powerfit_gb300 import synth
+    from powerfit_gb300.correlator import determine_core_indices
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    c = synth.make_case((n, n, n), vs, natoms, 2, 6.0, 4.0, 40 + n)
+    mask = determine_core_indices(c.mask) if laplace else c.mask
+    rot = quat_to_rotmat(super_fibonacci(7416))[::1854]       # 4 rotations of the 9.72 degree set's size
+    _parity(c.target.astype(np.float64), c.template, mask, rot, laplace, "%d^3" % n)

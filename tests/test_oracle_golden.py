@@ -101,3 +101,31 @@ def test_oracle_matches_live_reference():
         lcc, r = O.scan(p, rot)
         assert np.max(np.abs(lcc - corr.lcc)) < 1e-12
         assert np.array_equal(r, corr.rot)
+
+
+def test_reference_rotation_slice_matches_quat_to_rotmat():
+    """The 4.71 degree set slice (the reference's quaternions and its own
+    quat_to_rotmat of them): this package's quat_to_rotmat gives the same
+    matrices, element for element."""
+    from powerfit_gb300.rotations import quat_to_rotmat
+    d = np.load(os.path.join(GOLD, "rotset_471.npz"))
+    assert int(d["set_size"]) == 70728 and d["rows"].shape[0] == 2048
+    assert np.array_equal(quat_to_rotmat(d["quat"]), d["rotmats"])
+
+
+def test_top2_slices_merge_like_one_scan():
+    """Contiguous rotation slices merged with merge_top2 give the serial
+    scan's best LCC, best rotation and runner-up exactly."""
+    from powerfit_gb300 import synth
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    c = synth.make_case((16, 18, 20), 2.0, 150, 2, 8.0, 5.0, 5)
+    rot = quat_to_rotmat(super_fibonacci(11))
+    rot[4] = rot[3]                      # an exact tie across the slice boundary below
+    t = c.target.astype(np.float64)
+    p = O.prepare(t, c.template, c.mask, False)
+    ref = O.scan(p, rot, track_second=True)
+    offsets = [0, 4, 7]
+    parts = [O.scan(p, rot[o:e], track_second=True) for o, e in zip(offsets, offsets[1:] + [rot.shape[0]])]
+    got = O.merge_top2(parts, offsets)
+    for a, b in zip(ref, got):
+        assert np.array_equal(a, b)

@@ -1,6 +1,7 @@
 """Host side of the learned proposal (no GPU): the float64 network oracle
 against finite differences, rotation-set geometry, coarse maps."""
 import numpy as np
+import pytest
 
 from oracle import mlp
 
@@ -73,6 +74,32 @@ def test_checkpoint_file_round_trip(tmp_path):
     assert np.array_equal(l2, lcc) and np.array_equal(r2, rot) and (nxt, nrot) == (40, 100)
     checkpoint.save(path, lcc * 2, rot, 60, 100)          # replaced atomically
     assert checkpoint.load(path)[2] == 60
+
+
+def test_checkpoint_refuses_another_search(tmp_path):
+    """A checkpoint records its rotation set's digest and the rotation offset;
+    resuming with the same count but other rotations, or another offset, is
+    refused before any device call."""
+    from powerfit_gb300 import checkpoint
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+
+    class NoDevice:
+        def __getattr__(self, name):
+            raise AssertionError("device call %s before the checkpoint was checked" % name)
+
+    rot = quat_to_rotmat(super_fibonacci(30))
+    path = str(tmp_path / "c.npz")
+    lcc = np.zeros((4, 5, 6), np.float32)
+    checkpoint.save(path, lcc, lcc.astype(np.int32), 10, 30, checkpoint.rotation_digest(rot), 7)
+    assert checkpoint.load_identity(path) == (checkpoint.rotation_digest(rot), 7)
+    other = rot.copy()
+    other[3] = other[4]
+    with pytest.raises(ValueError, match="another rotation set"):
+        checkpoint.scan_resumable(NoDevice(), other, path, rot_offset=7)
+    with pytest.raises(ValueError, match="offset"):
+        checkpoint.scan_resumable(NoDevice(), rot, path, rot_offset=0)
+    with pytest.raises(ValueError, match="rotations"):
+        checkpoint.scan_resumable(NoDevice(), rot[:29], path, rot_offset=7)
 
 
 def test_best_rank_counts_rotations_scored_above_the_best_fit():
