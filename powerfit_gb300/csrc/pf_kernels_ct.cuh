@@ -199,6 +199,25 @@ struct SpectrumOperand {  // target spectrum plane [kz][ky] of this kx
   }
 };
 
+// Columns of the plane for the first forward z stage: rows of the zero band
+// (the z planes beyond the reach, zlo < z < hi) read as zeros without touching
+// shared memory, so the copy-in never stores them.
+struct BandCols {  // line = y (column), idx = z
+  const float2* base;
+  int rs, zlo, hi;
+  __device__ __forceinline__ float2 load(int line, int idx) const {
+    const float2* q = base + idx * rs + line;
+    const bool in = idx <= zlo || idx >= hi;
+    return (in && PF_CHECK_SMEM(kChkSmem, q, 8)) ? *q : make_float2(0.f, 0.f);
+  }
+};
+
+// Pass-2 copy-in: 1 (default) copies only the valid z rows and lets the first
+// z stage read the zero band as zeros (BandCols); 0 stores zeros in the band.
+#ifndef PF_P2_BAND
+#define PF_P2_BAND 1
+#endif
+
 // Block shape of the plane pass: a plane of 128 x 128 or more fills one block
 // per SM (shared memory), which then runs 1024 threads; smaller planes run two
 // 512-thread blocks per SM.  Both leave 64 registers a thread.
@@ -231,8 +250,11 @@ __global__ void __launch_bounds__(PlaneLaunch<Y, Z>::kThreads, PlaneLaunch<Y, Z>
 
   // copy-in: asynchronous 8-byte copies of the rows the rotation can reach,
   // zeros elsewhere (every thread keeps many copies in flight)
-  for (int v = threadIdx.x; v < Z * Y; v += kThreadsPlaneCt) {
-    const int z = v / Y, y = v - z * Y;
+  const bool band = PF_P2_BAND && p.mode == 0;
+  const int ncopy = band ? nvz * Y : Z * Y;    // band: the valid z rows only
+  for (int v = threadIdx.x; v < ncopy; v += kThreadsPlaneCt) {
+    const int i = v / Y, y = v - i * Y;
+    const int z = (band && i > lo_end) ? i + (Z - nvz) : i;
     const bool valid = p.mode != 0 ||
                        ((z <= lo_end || z >= hi_start) && row_in_disk(g, signed_coord(z, Z), signed_coord(y, Y), re2));
     if (!PF_CHECK_SMEM(kChkSmem, pl + z * rs + y, 8)) continue;
@@ -250,8 +272,12 @@ __global__ void __launch_bounds__(PlaneLaunch<Y, Z>::kThreads, PlaneLaunch<Y, Z>
   SmemLines cols{pl, 1, rs};
   if (p.mode == 0) {
     const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + (long long)kx * plane;
-    ct_fwd_mul_inv<Z, kThreadsPlaneCt, kEmax>(Y, twz, cols, SpectrumOperand{spec, Y, p.spec_len - (long long)kx * plane},
-                                              cols, true);
+    if (band)
+      ct_fwd_mul_inv<Z, kThreadsPlaneCt, kEmax>(Y, twz, cols, SpectrumOperand{spec, Y, p.spec_len - (long long)kx * plane},
+                                                BandCols{pl, rs, lo_end, hi_start}, true);
+    else
+      ct_fwd_mul_inv<Z, kThreadsPlaneCt, kEmax>(Y, twz, cols, SpectrumOperand{spec, Y, p.spec_len - (long long)kx * plane},
+                                                cols, true);
     // inverse y: all stages but the last in place, the last one straight to the buffer
     SmemLines allrows{pl, rs, 1};
     ct_head_inplace<Y, true, kThreadsPlaneCt, kEmax, 0>(Z, twy, allrows);
@@ -534,19 +560,26 @@ __device__ __forceinline__ void pass3_prefetch(const float2* __restrict__ base, 
 #ifndef PF_PASS3_EMAX
 #define PF_PASS3_EMAX 16
 #endif
+// 1: pass 3 instantiated with the tile rows 8 and 16 as compile-time constants
+#ifndef PF_P3_CT_TY
+#define PF_P3_CT_TY 1
+#endif
 constexpr int kThreadsPass3Ct = PF_PASS3_THREADS;
 constexpr int kVoxPass3Ct = (kMaxVoxPass3Fast + kThreadsPass3Ct - 1) / kThreadsPass3Ct;
 
-template <int X>
+// TY > 0: the tile rows as a compile-time constant (the launcher picks this
+// instantiation when p.ty == TY), so every tile index folds into constants;
+// TY == 0 reads them from p.ty.
+template <int X, int TY>
 __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct(const Pass3Params p) {
   constexpr int NT = kThreadsPass3Ct, VPT = kVoxPass3Ct;
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
-  const int ty = p.ty;                      // a power of two >= 2 on this path
+  const int ty = TY > 0 ? TY : p.ty;        // a power of two >= 2 on this path
   float2* tw = sm;
   unsigned short* s_list = reinterpret_cast<unsigned short*>(sm + X);
   float2* fbuf0 = sm + X + pass3_list_slots(X, ty);
-  const int sh = __ffs(ty) - 1;
+  const int sh = TY > 0 ? ct_log2(TY) : __ffs(ty) - 1;
   const int fbuf_stride = 3 * ty * X;
 
   const int z = blockIdx.x;
@@ -733,8 +766,17 @@ struct FastSize {
     // (planes beyond one block take the split path for the target spectra)
     if constexpr (plane_fits_block<N>()) k_pass2_ct<N, N><<<grid, PlaneLaunch<N, N>::kThreads, smem, s>>>(p, re2);
   }
+  // compile-time tile rows where a tile of that many rows fits the block
+  static constexpr bool kTy16 = PF_P3_CT_TY && 16 * N <= kMaxVoxPass3Fast;
+  static constexpr bool kTy8 = PF_P3_CT_TY && 8 * N <= kMaxVoxPass3Fast;
   static void pass3(const Pass3Params& p, dim3 grid, size_t smem, cudaStream_t s) {
-    k_pass3_ct<N><<<grid, kThreadsPass3Ct, smem, s>>>(p);
+    if constexpr (kTy16) {
+      if (p.ty == 16) { k_pass3_ct<N, 16><<<grid, kThreadsPass3Ct, smem, s>>>(p); return; }
+    }
+    if constexpr (kTy8) {
+      if (p.ty == 8) { k_pass3_ct<N, 8><<<grid, kThreadsPass3Ct, smem, s>>>(p); return; }
+    }
+    k_pass3_ct<N, 0><<<grid, kThreadsPass3Ct, smem, s>>>(p);
   }
   template <class K>
   static cudaError_t allow_smem(K kernel, size_t bytes) {
@@ -747,7 +789,13 @@ struct FastSize {
   // `smem_line` / `smem_plane`: total shared memory (static + dynamic) each kernel may use
   static cudaError_t set_attrs(size_t smem_line, size_t smem_plane) {
     cudaError_t e = allow_smem(k_pass1_ct<N>, smem_line);
-    if (e == cudaSuccess) e = allow_smem(k_pass3_ct<N>, smem_line);
+    if (e == cudaSuccess) e = allow_smem(k_pass3_ct<N, 0>, smem_line);
+    if constexpr (kTy16) {
+      if (e == cudaSuccess) e = allow_smem(k_pass3_ct<N, 16>, smem_line);
+    }
+    if constexpr (kTy8) {
+      if (e == cudaSuccess) e = allow_smem(k_pass3_ct<N, 8>, smem_line);
+    }
     if constexpr (plane_fits_block<N>()) {
       if (e == cudaSuccess) e = allow_smem(k_pass2_ct<N, N>, smem_plane);
     }
