@@ -13,6 +13,25 @@
 
 namespace pf {
 
+// Threads that run a transform together, and their barrier.  BlockTeam: the
+// whole block (__syncthreads).  GroupTeam<NTT>: the block split into teams of
+// NTT consecutive threads (whole warps), team t synchronising on named barrier
+// 1 + t alone, so that teams working on disjoint lines run their stages out of
+// step with each other (one team's loads beside another's arithmetic).
+struct BlockTeam {
+  static __device__ __forceinline__ int tid() { return threadIdx.x; }
+  static __device__ __forceinline__ void sync() { __syncthreads(); }
+};
+template <int NTT>
+struct GroupTeam {
+  static_assert(NTT % 32 == 0, "a team is whole warps");
+  static __device__ __forceinline__ int tid() { return threadIdx.x % NTT; }
+  static __device__ __forceinline__ int team() { return threadIdx.x / NTT; }
+  static __device__ __forceinline__ void sync() {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + (int)(threadIdx.x / NTT)), "n"(NTT) : "memory");
+  }
+};
+
 struct CtPlan {
   int n;
   int nst;
@@ -94,7 +113,7 @@ constexpr int ct_log2(int v) {
 // partial chunk of at most C/2 lines is mapped as C/2 lines: its items then
 // fill whole warps and the other warps wait at the barrier instead of issuing
 // with half their lanes off (48 lines: 32 + 16).
-template <int R, bool INV, int L, int NS, int NT, int EMAX, class Src, class Dst>
+template <int R, bool INV, int L, int NS, int NT, int EMAX, class TM = BlockTeam, class Src, class Dst>
 __device__ __forceinline__ void ct_stage(int nlines, const float2* __restrict__ tw, const Src& src, const Dst& dst,
                                          bool alias) {
   constexpr int NB = L / R;
@@ -116,7 +135,7 @@ __device__ __forceinline__ void ct_stage(int nlines, const float2* __restrict__ 
     float2 v[K][R];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      const int it = threadIdx.x + k * NT;
+      const int it = TM::tid() + k * NT;
       const int line = l0 + (it & cm);
       const int j = it >> sh;
       if (j < NB && line < nlines) {
@@ -134,10 +153,10 @@ __device__ __forceinline__ void ct_stage(int nlines, const float2* __restrict__ 
         DFT<R, INV>::run(v[k]);
       }
     }
-    if (alias) __syncthreads();
+    if (alias) TM::sync();
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      const int it = threadIdx.x + k * NT;
+      const int it = TM::tid() + k * NT;
       const int line = l0 + (it & cm);
       const int j = it >> sh;
       if (j < NB && line < nlines) {
@@ -146,11 +165,11 @@ __device__ __forceinline__ void ct_stage(int nlines, const float2* __restrict__ 
         for (int r = 0; r < R; ++r) dst.store(line, base + r * NS, v[k][r]);
       }
     }
-    if (alias) __syncthreads();
+    if (alias) TM::sync();
   }
 }
 
-template <int L, bool INV, int NT, int EMAX, int S, class Src, class Mid, class Dst>
+template <int L, bool INV, int NT, int EMAX, int S, class TM, class Src, class Mid, class Dst>
 __device__ __forceinline__ void ct_lines_from(int nlines, const float2* __restrict__ tw, const Src& src,
                                               const Mid& mid, const Dst& dst, bool src_alias, bool dst_alias) {
   constexpr CtPlan P = ct_plan(L);
@@ -158,57 +177,57 @@ __device__ __forceinline__ void ct_lines_from(int nlines, const float2* __restri
     constexpr int R = P.r[S];
     constexpr int NS = ct_stage_ns(L, S);
     if constexpr (P.nst == 1) {
-      ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, src, dst, src_alias || dst_alias);
+      ct_stage<R, INV, L, NS, NT, EMAX, TM>(nlines, tw, src, dst, src_alias || dst_alias);
     } else if constexpr (S == 0) {
-      ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, src, mid, src_alias);
-      __syncthreads();
+      ct_stage<R, INV, L, NS, NT, EMAX, TM>(nlines, tw, src, mid, src_alias);
+      TM::sync();
     } else if constexpr (S == P.nst - 1) {
-      ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, mid, dst, dst_alias);
+      ct_stage<R, INV, L, NS, NT, EMAX, TM>(nlines, tw, mid, dst, dst_alias);
     } else {
-      ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, mid, mid, true);
-      __syncthreads();
+      ct_stage<R, INV, L, NS, NT, EMAX, TM>(nlines, tw, mid, mid, true);
+      TM::sync();
     }
-    ct_lines_from<L, INV, NT, EMAX, S + 1>(nlines, tw, src, mid, dst, src_alias, dst_alias);
+    ct_lines_from<L, INV, NT, EMAX, S + 1, TM>(nlines, tw, src, mid, dst, src_alias, dst_alias);
   }
 }
 
 // Full length-L transform of `nlines` lines: first stage reads `src`, last
 // writes `dst`, the others work in `mid` (shared memory).  Ends with a barrier.
-template <int L, bool INV, int NT, int EMAX, class Src, class Mid, class Dst>
+template <int L, bool INV, int NT, int EMAX, class TM = BlockTeam, class Src, class Mid, class Dst>
 __device__ __forceinline__ void ct_lines(int nlines, const float2* __restrict__ tw, const Src& src, const Mid& mid,
                                          const Dst& dst, bool src_alias, bool dst_alias) {
-  ct_lines_from<L, INV, NT, EMAX, 0>(nlines, tw, src, mid, dst, src_alias, dst_alias);
-  __syncthreads();
+  ct_lines_from<L, INV, NT, EMAX, 0, TM>(nlines, tw, src, mid, dst, src_alias, dst_alias);
+  TM::sync();
 }
 
 
 // Forward stages 0 .. nst-2 in place (all but the last); stage 0 reads `src`
 // (which aliases `mid` when `src_alias`).
-template <int L, int NT, int EMAX, int S, class Src, class Mid>
+template <int L, int NT, int EMAX, int S, class TM, class Src, class Mid>
 __device__ __forceinline__ void ct_fwd_head(int nlines, const float2* __restrict__ tw, const Src& src,
                                             const Mid& mid, bool src_alias) {
   constexpr CtPlan P = ct_plan(L);
   if constexpr (S < P.nst - 1) {
     constexpr int R = P.r[S];
     constexpr int NS = ct_stage_ns(L, S);
-    if constexpr (S == 0) ct_stage<R, false, L, NS, NT, EMAX>(nlines, tw, src, mid, src_alias);
-    else ct_stage<R, false, L, NS, NT, EMAX>(nlines, tw, mid, mid, true);
-    __syncthreads();
-    ct_fwd_head<L, NT, EMAX, S + 1>(nlines, tw, src, mid, src_alias);
+    if constexpr (S == 0) ct_stage<R, false, L, NS, NT, EMAX, TM>(nlines, tw, src, mid, src_alias);
+    else ct_stage<R, false, L, NS, NT, EMAX, TM>(nlines, tw, mid, mid, true);
+    TM::sync();
+    ct_fwd_head<L, NT, EMAX, S + 1, TM>(nlines, tw, src, mid, src_alias);
   }
 }
 
 // Stages 0 .. nst-2 of a length-L transform, in place in `mid`, each followed
 // by a barrier.
-template <int L, bool INV, int NT, int EMAX, int S, class Mid>
+template <int L, bool INV, int NT, int EMAX, int S, class TM = BlockTeam, class Mid>
 __device__ __forceinline__ void ct_head_inplace(int nlines, const float2* __restrict__ tw, const Mid& mid) {
   constexpr CtPlan P = ct_plan(L);
   if constexpr (S < P.nst - 1) {
     constexpr int R = P.r[S];
     constexpr int NS = ct_stage_ns(L, S);
-    ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, mid, mid, true);
-    __syncthreads();
-    ct_head_inplace<L, INV, NT, EMAX, S + 1>(nlines, tw, mid);
+    ct_stage<R, INV, L, NS, NT, EMAX, TM>(nlines, tw, mid, mid, true);
+    TM::sync();
+    ct_head_inplace<L, INV, NT, EMAX, S + 1, TM>(nlines, tw, mid);
   }
 }
 
@@ -230,14 +249,14 @@ __device__ __forceinline__ void ct_last_twiddles(const float2* __restrict__ tw, 
 // `mid` and writing `out`.  Its stores y[j + r Ns] from consecutive threads
 // cover consecutive elements of a line, so `out` may be global memory, written
 // in whole segments straight from registers.  `tl` is the [r][j] table above.
-template <int L, bool INV, int NT, class Mid, class Out>
+template <int L, bool INV, int NT, class TM = BlockTeam, class Mid, class Out>
 __device__ __forceinline__ void ct_last_stage_out(int nlines, const float2* __restrict__ tl, const Mid& mid,
                                                   const Out& out) {
   constexpr CtPlan P = ct_plan(L);
   constexpr int R = P.r[P.nst - 1];
   constexpr int NB = L / R;
   const int total = nlines * NB;
-  for (int it = threadIdx.x; it < total; it += NT) {
+  for (int it = TM::tid(); it < total; it += NT) {
     const int line = it / NB, j = it - line * NB;
     float2 v[R];
 #pragma unroll
@@ -276,7 +295,8 @@ constexpr int ct_stage_ns_rev(int n, int stage) {
 // Stages S .. nst-1 of the reversed plan, in place in `mid`; the last one
 // stores to `dst` instead when `kToDst` (a different memory: no barrier
 // between its loads and stores, none after it).
-template <int L, bool INV, int NT, int EMAX, int S, bool kToDst = false, class Mid, class Dst = Mid>
+template <int L, bool INV, int NT, int EMAX, int S, bool kToDst = false, class TM = BlockTeam, class Mid,
+          class Dst = Mid>
 __device__ __forceinline__ void ct_rev_from(int nlines, const float2* __restrict__ tw, const Mid& mid,
                                             const Dst& dst = Dst{}) {
   constexpr CtPlan Q = ct_plan_rev(L);
@@ -284,11 +304,11 @@ __device__ __forceinline__ void ct_rev_from(int nlines, const float2* __restrict
     constexpr int R = Q.r[S];
     constexpr int NS = ct_stage_ns_rev(L, S);
     if constexpr (kToDst && S == Q.nst - 1) {
-      ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, mid, dst, false);
+      ct_stage<R, INV, L, NS, NT, EMAX, TM>(nlines, tw, mid, dst, false);
     } else {
-      ct_stage<R, INV, L, NS, NT, EMAX>(nlines, tw, mid, mid, true);
-      __syncthreads();
-      ct_rev_from<L, INV, NT, EMAX, S + 1, kToDst>(nlines, tw, mid, dst);
+      ct_stage<R, INV, L, NS, NT, EMAX, TM>(nlines, tw, mid, mid, true);
+      TM::sync();
+      ct_rev_from<L, INV, NT, EMAX, S + 1, kToDst, TM>(nlines, tw, mid, dst);
     }
   }
 }
@@ -304,7 +324,7 @@ __device__ __forceinline__ void ct_rev_from(int nlines, const float2* __restrict
 //
 // With a `Dst` other than `void`, the inverse's last stage stores to `dst`
 // (the plan must have at least two stages) and no barrier follows it.
-template <int L, int NT, int EMAX, class Mid, class Mul, class Src = Mid, class Dst = void>
+template <int L, int NT, int EMAX, class TM = BlockTeam, class Mid, class Mul, class Src = Mid, class Dst = void>
 __device__ __forceinline__ void ct_fwd_mul_inv(int nlines, const float2* __restrict__ tw, const Mid& mid,
                                                const Mul& mul, const Src& src, bool src_alias,
                                                const Dst* dstp = nullptr) {
@@ -312,7 +332,7 @@ __device__ __forceinline__ void ct_fwd_mul_inv(int nlines, const float2* __restr
   constexpr int RL = P.r[P.nst - 1];
   constexpr int NB = L / RL;
   // forward stages 0 .. nst-2
-  ct_fwd_head<L, NT, EMAX, 0>(nlines, tw, src, mid, src_alias);
+  ct_fwd_head<L, NT, EMAX, 0, TM>(nlines, tw, src, mid, src_alias);
   // fused stage
   constexpr int KMAX = (EMAX / RL) > 0 ? (EMAX / RL) : 1;
   constexpr int C0 = (NT * KMAX) / NB;
@@ -322,7 +342,7 @@ __device__ __forceinline__ void ct_fwd_mul_inv(int nlines, const float2* __restr
     float2 v[K][RL];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      const int it = threadIdx.x + k * NT;
+      const int it = TM::tid() + k * NT;
       const int line = l0 + (it & (C - 1));
       const int j = it / C;
       if (j < NB && line < nlines) {
@@ -346,10 +366,10 @@ __device__ __forceinline__ void ct_fwd_mul_inv(int nlines, const float2* __restr
         DFT<RL, true>::run(v[k]);         // inverse first stage (Ns = 1): no twiddles
       }
     }
-    __syncthreads();
+    TM::sync();
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      const int it = threadIdx.x + k * NT;
+      const int it = TM::tid() + k * NT;
       const int line = l0 + (it & (C - 1));
       const int j = it / C;
       if (j < NB && line < nlines) {
@@ -357,14 +377,14 @@ __device__ __forceinline__ void ct_fwd_mul_inv(int nlines, const float2* __restr
         for (int r = 0; r < RL; ++r) mid.store(line, j * RL + r, v[k][r]);
       }
     }
-    __syncthreads();
+    TM::sync();
   }
   // inverse stages 1 .. nst-1 of the reversed plan
   if constexpr (std::is_void<Dst>::value) {
-    ct_rev_from<L, true, NT, EMAX, 1>(nlines, tw, mid);
+    ct_rev_from<L, true, NT, EMAX, 1, false, TM>(nlines, tw, mid);
   } else {
     static_assert(P.nst >= 2, "the last inverse stage must not be the fused one");
-    ct_rev_from<L, true, NT, EMAX, 1, true>(nlines, tw, mid, *dstp);
+    ct_rev_from<L, true, NT, EMAX, 1, true, TM>(nlines, tw, mid, *dstp);
   }
 }
 

@@ -212,6 +212,33 @@ struct BandCols {  // line = y (column), idx = z
   }
 };
 
+// Rows of the valid z planes from valid row i0 on (line l -> valid row i0 + l)
+struct RowMapLinesOff {
+  float2* base;
+  int rs, zlo, shift, i0;
+  __device__ __forceinline__ int row(int l) const {
+    const int i = i0 + l;
+    return i <= zlo ? i : i + shift;
+  }
+  __device__ __forceinline__ float2 load(int line, int idx) const {
+    const float2* q = base + row(line) * rs + idx;
+    return PF_CHECK_SMEM(kChkSmem, q, 8) ? *q : make_float2(0.f, 0.f);
+  }
+  __device__ __forceinline__ void store(int line, int idx, float2 v) const {
+    float2* q = base + row(line) * rs + idx;
+    if (PF_CHECK_SMEM(kChkSmem, q, 8)) *q = v;
+  }
+};
+
+// Plane pass in teams: 1 (default) splits the block into teams of four warps
+// where the plane is square and its lines split into 16 per team (64^2 and
+// 128^2 planes); each team transforms its own 16 rows or columns and waits on
+// its own barrier, with block barriers only where the transform direction
+// changes (rows -> columns -> rows).  0: every stage block-wide.
+#ifndef PF_P2_GROUPS
+#define PF_P2_GROUPS 1
+#endif
+
 // Pass-2 copy-in: 1 (default) copies only the valid z rows and lets the first
 // z stage read the zero band as zeros (BandCols); 0 stores zeros in the band.
 #ifndef PF_P2_BAND
@@ -267,6 +294,36 @@ __global__ void __launch_bounds__(PlaneLaunch<Y, Z>::kThreads, PlaneLaunch<Y, Z>
   cp_async_wait_all();
   __syncthreads();
 
+  // teams of four warps owning 16 lines each (see PF_P2_GROUPS)
+  constexpr int kTeam = 128, kLinesTeam = 16;
+  constexpr bool kGroups = PF_P2_GROUPS && Y == Z && (Y / kLinesTeam) * kTeam == kThreadsPlaneCt;
+  if constexpr (kGroups) {
+    if (p.mode == 0) {
+      using TM = GroupTeam<kTeam>;
+      const int t = TM::team();
+      const int l0 = kLinesTeam * t;
+      // forward y: the team's valid rows l0 .. l0 + 15
+      RowMapLinesOff vrows{pl, rs, g.zlo, Z - nvz, l0};
+      ct_lines<Y, false, kTeam, kEmax, TM>(max(0, min(kLinesTeam, nvz - l0)), twy, vrows, vrows, vrows, true, true);
+      __syncthreads();                       // every valid row transformed
+      // z: the team's columns l0 .. l0 + 15 -- forward, product, inverse
+      const long long spec_off = (long long)kx * plane + l0;
+      const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + spec_off;
+      SmemLines tcols{pl + l0, 1, rs};
+      const SpectrumOperand op{spec, Y, p.spec_len - spec_off};
+      if (band)
+        ct_fwd_mul_inv<Z, kTeam, kEmax, TM>(kLinesTeam, twz, tcols, op, BandCols{pl + l0, rs, lo_end, hi_start}, true);
+      else
+        ct_fwd_mul_inv<Z, kTeam, kEmax, TM>(kLinesTeam, twz, tcols, op, tcols, true);
+      __syncthreads();                       // every column transformed
+      // inverse y: the team's rows l0 .. l0 + 15, the last stage straight to the buffer
+      SmemLines trows{pl + l0 * rs, rs, 1};
+      ct_head_inplace<Y, true, kTeam, kEmax, 0, TM>(kLinesTeam, twy, trows);
+      ct_last_stage_out<Y, true, kTeam, TM>(kLinesTeam, tly, trows,
+                                             GlobalRows{gplane + (long long)l0 * Y, Y, glim - (long long)l0 * Y});
+      return;
+    }
+  }
   RowMapLines rows{pl, rs, g.zlo, Z - nvz};
   ct_lines<Y, false, kThreadsPlaneCt, kEmax>(nvz, twy, rows, rows, rows, true, true);
   SmemLines cols{pl, 1, rs};
