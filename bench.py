@@ -687,7 +687,8 @@ def run_kernels(args):
     """One launch of every kernel outside the fast search passes, at 128^3:
     GPU preprocessing (splat, dilation, Laplace, core weights), the
     runtime-planned search passes and target spectra (PF_FLAG_GENERIC), the
-    same passes with the DFT stages on the tensor cores (PF_FLAG_TENSOR_DFT),
+    same passes with the DFT stages on the tensor cores (PF_FLAG_TENSOR_DFT:
+    mma.sync; with PF_FLAG_TENSOR_TC05 the plane pass's stages on tcgen05),
     the float64 unit mirrors, the shard merge and the proposal network's kernels.
     Wall time per call (synchronised); meant as the command an ncu capture
     of these kernels runs."""
@@ -728,6 +729,8 @@ def run_kernels(args):
     rot = quat_to_rotmat(super_fibonacci(8))
     timed("scan generic", lambda: ctx.scan(rot, flags=_lib.PF_FLAG_GENERIC))
     timed("scan tensor-core DFT", lambda: ctx.scan(rot, flags=_lib.PF_FLAG_TENSOR_DFT))
+    timed("scan tensor-core DFT, tcgen05 plane pass",
+          lambda: ctx.scan(rot, flags=_lib.PF_FLAG_TENSOR_DFT | _lib.PF_FLAG_TENSOR_TC05))
     lcc, r = ctx.scan(rot[:2])
     timed("combine", lambda: _lib.combine_into(lcc.copy(), r.copy(), lcc, r, 0))
     timed("fft3d", lambda: ctx.fft3d(target.astype(np.float32)))

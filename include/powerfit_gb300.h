@@ -43,6 +43,9 @@ extern "C" {
 #define PF_FLAG_ROT_MAX 16    /* also keep, per rotation, the best LCC over the lcc-mask voxels (pf_get_rotation_max) */
 #define PF_FLAG_TENSOR_DFT 32 /* precision study: the DFT stages of the search on the tensor cores in split-bf16x3
                                  (mma.sync bf16, float32 accumulation; runtime-planned kernels, edges <= 256) */
+#define PF_FLAG_TENSOR_TC05 64 /* with PF_FLAG_TENSOR_DFT: the plane pass's DFT stages with tcgen05.mma (operands
+                                  in shared memory, accumulators in tensor memory) instead of mma.sync; planes that
+                                  fit one block with the operand area (PF_E_ARG otherwise) */
 
 typedef struct pf_ctx pf_ctx;
 

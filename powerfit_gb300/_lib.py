@@ -27,6 +27,7 @@ PF_FLAG_ACCUMULATE = 4
 PF_FLAG_GENERIC = 8
 PF_FLAG_ROT_MAX = 16
 PF_FLAG_TENSOR_DFT = 32
+PF_FLAG_TENSOR_TC05 = 64
 
 EXPORTS = [
     "pf_create", "pf_destroy", "pf_last_error", "pf_global_error", "pf_set_target",

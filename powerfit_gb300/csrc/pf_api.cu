@@ -348,6 +348,7 @@ int set_smem_limits(pf_ctx* c) {
   PF_CUDA(c, allow_smem(k_pass1<true>, m));
   PF_CUDA(c, allow_smem(k_pass3<true>, m));
   PF_CUDA(c, allow_smem(k_pass2<true>, m));
+  PF_CUDA(c, allow_smem(k_pass2<2>, m));
   PF_CUDA(c, allow_smem(k_split_rows<true>, m));
   PF_CUDA(c, allow_smem(k_split_cols<true>, m));
   if (c->fast) PF_CUDA(c, c->fl.set_attrs(m, m));
@@ -804,7 +805,14 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
   const int ty1 = c->ty1, ty3 = c->ty3;
   const size_t s1 = line_smem(c->nx, 3, ty1), s3 = line_smem(c->nx, 3, ty3), s2 = plane_smem(c->ny, c->nz);
   const bool tc = (flags & PF_FLAG_TENSOR_DFT) != 0;
+  const bool tc05 = tc && (flags & PF_FLAG_TENSOR_TC05) != 0;
   const bool fast = c->fast && !(flags & PF_FLAG_GENERIC) && !tc;
+  if (tc05) {
+    if (c->split || pass2_tc05_smem(s2) > c->max_smem)
+      return fail(c, PF_E_ARG, "PF_FLAG_TENSOR_TC05: the (z, y) plane and the tcgen05 operands exceed shared memory");
+    const int zero = 0;
+    PF_CUDA(c, cudaMemcpyToSymbolAsync(g_tc05_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, c->stream));
+  }
   const int re = std::min(g.rmax, g.reff);
   const int re2 = re * re;
   const int64_t end = first + count;
@@ -850,7 +858,8 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
         launch_split_pass2(c, g, npairs, 3, 0, nullptr, 1.0f, tc);   // rows, columns, rows
         return 3;
       }
-      if (tc) k_pass2<true><<<g2, kThreadsPlane, s2, c->stream>>>(p2);
+      if (tc05) k_pass2<2><<<g2, kThreadsPlane, pass2_tc05_smem(s2), c->stream>>>(p2);
+      else if (tc) k_pass2<true><<<g2, kThreadsPlane, s2, c->stream>>>(p2);
       else k_pass2<false><<<g2, kThreadsPlane, s2, c->stream>>>(p2);
       return 1;
     });
@@ -892,6 +901,12 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
       return 1;
     });
     if (rc) return rc;
+  }
+  if (tc05) {   // a tensor-core wait that ran out in any block of the plane pass
+    int err = 0;
+    PF_CUDA(c, cudaMemcpyFromSymbolAsync(&err, g_tc05_error, sizeof(int), 0, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (err) return fail(c, PF_E_CUDA, "PF_FLAG_TENSOR_TC05: a wait for the tensor-core products ran out");
   }
   return PF_OK;
 }

@@ -333,12 +333,23 @@ template <bool INV, class Src, class Dst>
 __device__ __noinline__ void fft_stage_mma(int R, int nlines, int L, int Ns, const float2* __restrict__ tw,
                                            const Src src, const Dst dst, bool alias);
 
-// TC: the R-point DFTs on the tensor cores in split-bf16x3 (a precision-study
-// variant), else in float32 codelets
-template <bool INV, int EMAX, bool TC, class Src, class Dst>
+// split-bf16x3 stage on the tcgen05 tensor cores (pf_fft_tc05.cuh)
+template <bool INV, class Src, class Dst>
+__device__ __noinline__ void fft_stage_tc05(int R, int nlines, int L, int Ns, const float2* __restrict__ tw,
+                                            const Src src, const Dst dst, bool alias);
+
+// TC: 0, the R-point DFTs in float32 codelets; 1, on the tensor cores in
+// split-bf16x3 with mma.sync; 2, the same products with tcgen05.mma (both
+// precision-study variants)
+template <bool INV, int EMAX, int TC, class Src, class Dst>
 __device__ __noinline__ void fft_stage_rt(int R, int nlines, int L, int Ns, const float2* __restrict__ tw,
                                           const Src src, const Dst dst, bool alias) {
-  if constexpr (TC) {
+  if constexpr (TC == 2) {
+    if (R > 1) {
+      fft_stage_tc05<INV>(R, nlines, L, Ns, tw, src, dst, alias);
+      return;
+    }
+  } else if constexpr (TC == 1) {
     if (R > 1) {
       fft_stage_mma<INV>(R, nlines, L, Ns, tw, src, dst, alias);
       return;
@@ -362,7 +373,7 @@ __device__ __noinline__ void fft_stage_rt(int R, int nlines, int L, int Ns, cons
 // Full transform of `nlines` lines of length pl.n: the first stage reads from
 // `src`, the last writes to `dst`, intermediate stages work in `mid` (shared
 // memory).  `src_alias`/`dst_alias`: whether src/dst share storage with `mid`.
-template <bool INV, int EMAX, bool TC = false, class Src, class Mid, class Dst>
+template <bool INV, int EMAX, int TC = 0, class Src, class Mid, class Dst>
 __device__ __forceinline__ void fft_lines(const AxisPlan& pl, int nlines, const float2* __restrict__ tw,
                                           const Src src, const Mid mid, const Dst dst,
                                           bool src_alias, bool dst_alias) {

@@ -27,6 +27,7 @@
 
 #include "pf_fft.cuh"
 #include "pf_fft_mma.cuh"
+#include "pf_fft_tc05.cuh"
 
 namespace pf {
 
@@ -308,8 +309,16 @@ struct ProductStore {  // column transforms: line = ky, idx = kz
   }
 };
 
+// Shared memory of the tcgen05 plane pass: the plane (plane_smem), then the
+// operand area of the tensor-core stages on a 1024-byte boundary.
+__host__ __device__ inline size_t pass2_tc05_smem(size_t plane_bytes) {
+  return plane_bytes + 1024 + kTc05SmemBytes;
+}
+
 #ifdef PF_GENERIC_KERNELS
-template <bool TC>
+// TC: 0 float32 stages; 1 split-bf16x3 mma.sync stages; 2 split-bf16x3
+// tcgen05 stages (operands in shared memory after the plane)
+template <int TC>
 __global__ void __launch_bounds__(kThreadsPlane) k_pass2(const Pass2Params p) {
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
@@ -320,6 +329,13 @@ __global__ void __launch_bounds__(kThreadsPlane) k_pass2(const Pass2Params p) {
   const int rs = Y + kPad;
   for (int i = threadIdx.x; i < Y; i += blockDim.x) twy[i] = p.twy[i];
   for (int i = threadIdx.x; i < Z; i += blockDim.x) twz[i] = p.twz[i];
+  if constexpr (TC == 2) {
+    static_assert(kThreadsPlane == kTc05Threads, "the tcgen05 stages map one item per thread of the plane pass");
+    const size_t plane_end = (size_t)(Y + Z + (size_t)Z * rs) * sizeof(float2);
+    const unsigned int base = smem_u32(sm);
+    const unsigned int ops = (base + (unsigned int)plane_end + 1023u) & ~1023u;
+    tc05_begin(reinterpret_cast<char*>(sm) + (ops - base));
+  }
 
   const int kx = blockIdx.x, f = blockIdx.y, pair = blockIdx.z;
   const long long plane = (long long)Z * Y;
@@ -353,6 +369,7 @@ __global__ void __launch_bounds__(kThreadsPlane) k_pass2(const Pass2Params p) {
       const long long i = (long long)z * Y + y;
       if (PF_CHECK(kChkBufStore, i, glim) && PF_CHECK_SMEM(kChkSmem, pl + z * rs + y, 8)) gplane[i] = pl[z * rs + y];
     }
+    if constexpr (TC == 2) tc05_end();
   } else {
     fft_lines<false, kEmax, TC>(p.pz, Y, twz, cols, cols, cols, true, true);
     const long long out_off = ((long long)f * g.nx + kx) * plane;
@@ -363,6 +380,7 @@ __global__ void __launch_bounds__(kThreadsPlane) k_pass2(const Pass2Params p) {
       if (PF_CHECK(kChkOut, i, p.out_len - out_off) && PF_CHECK_SMEM(kChkSmem, pl + z * rs + y, 8))
         o[i] = cscale(pl[z * rs + y], p.scale);
     }
+    if constexpr (TC == 2) tc05_end();
   }
 }
 

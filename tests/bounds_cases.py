@@ -15,8 +15,8 @@ kernels on tiny and odd grids (4x5x6, 5x6x7, 8^3, 10x12x14, 15x16x21,
 40x48x36), the compile-time kernels of every specialised size (32 .. 160),
 the clustered plane pass (192^3), the three-step plane pass (192x192x12),
 pruning on and off, the per-rotation maxima, float64 normalisation, the
-tensor-core DFT stages of the precision study, and batch and tile shapes
-other than the defaults.
+tensor-core DFT stages of the precision study (mma.sync, and tcgen05 in the
+plane pass), and batch and tile shapes other than the defaults.
 """
 from __future__ import annotations
 
@@ -30,7 +30,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-FP64, NO_PRUNE, GENERIC, ROT_MAX, TENSOR_DFT = 1, 2, 8, 16, 32
+FP64, NO_PRUNE, GENERIC, ROT_MAX, TENSOR_DFT, TENSOR_TC05 = 1, 2, 8, 16, 32, 64
 
 # name, shape, inputs ("rand": uniform noise, "synth": seeded map), rotations,
 # flags, tuning (pairs per batch, pass-1 rows, pass-3 rows; 0: default) or None
@@ -52,6 +52,8 @@ CASES = [
     ("split_192x192x12", (192, 192, 12), "synth", 6, 0, None),
     ("tensor_dft_48", (48, 48, 48), "synth", 10, TENSOR_DFT, None),
     ("tensor_dft_split", (192, 192, 12), "synth", 6, TENSOR_DFT, None),
+    ("tensor_tc05_48", (48, 48, 48), "synth", 10, TENSOR_DFT | TENSOR_TC05, None),
+    ("tensor_tc05_40x36x30", (40, 36, 30), "synth", 10, TENSOR_DFT | TENSOR_TC05, None),
 ]
 
 # cases re-run with a shrunk buffer extent (the checks must report accesses)

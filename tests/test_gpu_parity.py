@@ -294,6 +294,31 @@ def test_tensor_dft_variant_against_oracle(lib, shape):
     assert err_fp32 <= err_tc
 
 
+@pytest.mark.parametrize("shape", [(48, 48, 48), (40, 36, 30), (128, 128, 128)])
+def test_tensor_dft_tcgen05_against_oracle(lib, shape):
+    """The precision-study variant with the plane pass's DFT stages on the
+    fifth-generation tensor cores (tcgen05.mma, operands by shared-memory
+    descriptors, accumulators in tensor memory; PF_FLAG_TENSOR_DFT |
+    PF_FLAG_TENSOR_TC05): the same split-bf16x3 products as the mma.sync form,
+    so the same bound against the oracle."""
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    from powerfit_gb300._lib import PF_FLAG_TENSOR_DFT, PF_FLAG_TENSOR_TC05
+    from powerfit_gb300 import synth
+    vs = 2.0 if shape[0] < 100 else 1.5
+    c = synth.make_case(shape, vs, 500 if shape[0] < 100 else 2000, 2, 8.0, 5.0, 31)
+    rot = quat_to_rotmat(super_fibonacci(96))[::8]
+    target = c.target.astype(np.float64)
+    ref, ref_rot, second = O.scan_top2_parallel(target, c.template, c.mask, rot, False)
+    corr = correlator(target, c.template, c.mask, rot, False, flags=PF_FLAG_TENSOR_DFT | PF_FLAG_TENSOR_TC05)
+    fin = np.isfinite(ref)
+    err = float(np.max(np.abs(corr.lcc[fin] - ref[fin])))
+    clear = fin & ((ref - second) > 1e-4) & (ref > 0)
+    agree = float(np.mean(corr.rot[clear] == ref_rot[clear]))
+    print("%s tcgen05 split-bf16x3 max|dLCC| %.2e, argmax %.5f of %d clear voxels" % (shape, err, agree,
+                                                                                  int(clear.sum())))
+    assert err < TENSOR_DFT_LCC_BOUND and agree >= 0.999
+
+
 def test_split_plane_path_vs_oracle(lib):
     """(z, y) planes larger than shared memory take the three-step pass 2."""
     from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
