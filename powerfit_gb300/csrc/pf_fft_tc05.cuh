@@ -25,9 +25,10 @@
 // (tcgen05.ld 32x32b) and stores the R outputs in Stockham order.
 //
 // The block allocates 128 tensor-memory columns once (tc05_begin) and frees
-// them before it exits (tc05_end).  A wait that runs out (about a second of
-// polling) records an error in g_tc05_error and the block goes on without the
-// result, so the search returns an error instead of hanging.
+// them before it exits (tc05_end).  A wait that runs out (2 s on the global
+// timer) records an error in g_tc05_error; the block then skips its remaining
+// chunks, waits once more (bounded) for the products in flight and frees the
+// tensor memory, so the search returns an error instead of hanging.
 #pragma once
 #include <cuda_bf16.h>
 
@@ -42,7 +43,7 @@ constexpr int kTc05TileBytes = 128 * 32 * 2;       // one bf16 A tile (M = 128, 
 constexpr int kTc05BBytes = 32 * 32 * 2;           // one bf16 B matrix (N = 32, K = 32)
 // shared memory of the operands: A hi + lo of every tile, B hi + lo
 constexpr int kTc05SmemBytes = 2 * kTc05Tiles * kTc05TileBytes + 2 * kTc05BBytes;
-constexpr unsigned int kTc05WaitLimit = 1u << 26;  // mbarrier polls before a wait gives up
+constexpr unsigned long long kTc05WaitNs = 2000000000ull;  // a wait gives up after 2 s
 
 // per-block state of the tcgen05 stages
 struct Tc05State {
@@ -152,17 +153,26 @@ __device__ __forceinline__ void tc05_mma(unsigned int d, unsigned long long a, u
 }
 
 // Bounded wait for completion `parity` of the barrier; false if it ran out.
+// Non-blocking tests against the global nanosecond timer, about two seconds
+// at most (mbarrier.try_wait may suspend the thread for a system-dependent
+// time per call, so a count of calls bounds nothing).
+__device__ __forceinline__ unsigned long long tc05_now() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 __device__ __forceinline__ bool tc05_wait(unsigned int mbar, unsigned int parity) {
-  for (unsigned int i = 0; i < kTc05WaitLimit; ++i) {
+  const unsigned long long t0 = tc05_now();
+  for (;;) {
     unsigned int done;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
         : "r"(mbar), "r"(parity)
         : "memory");
     if (done) return true;
+    if (tc05_now() - t0 > kTc05WaitNs) return false;
   }
-  return false;
 }
 
 // One radix-R stage (2 <= R <= 16) of `nlines` lines of length L (the

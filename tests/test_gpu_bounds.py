@@ -70,7 +70,14 @@ def test_checked_equals_unchecked_and_oracle(checked_run, i):
     lcc, rot, rmax = B.run_case(_lib, i)
     c_lcc, c_rot = d[name + "_lcc"], d[name + "_rot"]
     diff = np.abs(c_lcc.astype(np.float64) - lcc)
-    assert np.max(diff) <= 1e-6, (name, float(np.max(diff)))
+    # The tcgen05 stages split each float32 operand into bfloat16 hi + lo:
+    # that split jumps at bf16 rounding boundaries, so a one-ulp difference in
+    # a twiddled input (the two builds may contract a multiply-add
+    # differently) can move a result by about the variant's own error against
+    # the oracle (1e-5 to 3e-5, measured); the builds are compared at that
+    # scale there, at 1e-6 everywhere else.
+    tol = 5e-5 if flags & B.TENSOR_TC05 else 1e-6
+    assert np.max(diff) <= tol, (name, float(np.max(diff)))
     same = diff == 0
     assert np.array_equal(c_rot[same], rot[same]), name
     if rmax is not None:
