@@ -848,8 +848,6 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     p2.mode = 0;
     p2.buf_len = buf_extent(c);
     p2.spec_len = c->N;
-    p2.persist = c->num_sms;
-    p2.smem_max = c->max_smem;
     dim3 g2(c->nx, 3, npairs);
     rc = timed_launch(c, 1, [&] {
       if (fast) {

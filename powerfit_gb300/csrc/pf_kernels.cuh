@@ -280,8 +280,6 @@ struct Pass2Params {
   long long buf_len = 0;          // elements of buf, of s1 and of s2, of out (bounds checks)
   long long spec_len = 0;
   long long out_len = 0;
-  int persist = 0;                // fast path, mode 0: blocks of the persistent plane pass (0: a block a plane)
-  size_t smem_max = 0;            // shared memory a block may use (persistent plane pass)
 };
 
 struct RowMapLines {  // line l -> data row (valid planes only), element idx along y

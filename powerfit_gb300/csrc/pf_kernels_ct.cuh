@@ -355,104 +355,6 @@ __global__ void __launch_bounds__(PlaneLaunch<Y, Z>::kThreads, PlaneLaunch<Y, Z>
 }
 
 // ---------------------------------------------------------------------------
-// Pass 2 (fast, persistent, mode 0): one block per SM walks the planes
-// q = blockIdx.x, blockIdx.x + gridDim.x, ... (q = (pair * nfield + f) * nx +
-// kx), in the teams of k_pass2_ct.  Beside the plane it keeps a staging area
-// of nvz rows: the valid rows of the next plane are copied in there while the
-// current plane runs its z and inverse-y stages, so the copy-in's memory
-// latency overlaps the transforms.  The forward y transform's first stage
-// reads the staging rows and writes the plane's (different memory: no barrier
-// between its loads and stores); after it the staging area is free for the
-// next plane.
-// ---------------------------------------------------------------------------
-#ifndef PF_P2_PERSIST
-#define PF_P2_PERSIST 1
-#endif
-
-template <int Y, int Z>
-__host__ __device__ constexpr size_t pass2_pst_smem(int nvz) {
-  return ((size_t)2 * Y + Z + (size_t)Z * (Y + kPad) + (size_t)nvz * (Y + kPad)) * sizeof(float2);
-}
-
-// valid rows of plane q into the staging area of the persistent plane pass:
-// 8-byte asynchronous copies of the entries the rotation can reach, zeros
-// elsewhere; one commit group
-template <int Y, int Z, int NT>
-__device__ __noinline__ void pass2_stage_in(const Pass2Params& p, int re2, int q, float2* stg) {
-  const Geometry& g = p.g;
-  constexpr int rs = Y + kPad;
-  const int nvz = g.nvz;
-  const long long off = (long long)q * Z * Y;    // planes are consecutive in buf
-  const float2* gp = p.buf + off;
-  const long long lim = p.buf_len - off;
-  for (int v = threadIdx.x; v < nvz * Y; v += NT) {
-    const int i = v / Y, y = v - i * Y;
-    const int z = i > g.zlo ? i + (Z - nvz) : i;
-    float2* d = stg + i * rs + y;
-    if (!PF_CHECK_SMEM(kChkSmem, d, 8)) continue;
-    if (row_in_disk(g, signed_coord(z, Z), signed_coord(y, Y), re2) && PF_CHECK(kChkBufLoad, (long long)z * Y + y, lim))
-      cp_async8(d, gp + (long long)z * Y + y);
-    else
-      *d = make_float2(0.f, 0.f);
-  }
-  cp_async_commit();
-}
-
-template <int Y, int Z>
-__global__ void __launch_bounds__(PlaneLaunch<Y, Z>::kThreads, 1)
-    k_pass2_pst(const Pass2Params p, const int re2, const int nplanes) {
-  constexpr int NT = PlaneLaunch<Y, Z>::kThreads;
-  constexpr int kTeam = 128, kLinesTeam = 16;
-  static_assert(Y == Z && (Y / kLinesTeam) * kTeam == NT, "teams of 16 lines must cover the plane");
-  using TM = GroupTeam<kTeam>;
-  extern __shared__ float2 sm[];
-  constexpr int rs = Y + kPad;
-  constexpr long long plane = (long long)Z * Y;
-  float2* twy = sm;
-  float2* twz = sm + Y;
-  float2* pl = sm + Y + Z;       // [Z][rs]
-  float2* tly = pl + Z * rs;     // last inverse-y stage twiddles, [r][j]
-  float2* stg = tly + Y;         // staging: [nvz][rs], the next plane's valid rows
-
-  if ((int)blockIdx.x < nplanes) pass2_stage_in<Y, Z, NT>(p, re2, blockIdx.x, stg);
-  for (int i = threadIdx.x; i < Y; i += NT) twy[i] = p.twy[i];
-  for (int i = threadIdx.x; i < Z; i += NT) twz[i] = p.twz[i];
-  ct_last_twiddles<Y, NT>(p.twy, tly);
-  for (int q = blockIdx.x; q < nplanes; q += gridDim.x) {
-    cp_async_wait_all();
-    __syncthreads();                         // plane q staged; every team done with the previous plane
-    const Geometry& g = p.g;
-    const int nvz = g.nvz;
-    const int l0 = kLinesTeam * TM::team();
-    // forward y: the team's valid rows, staging -> plane
-    {
-      SmemLines srows{stg + l0 * rs, rs, 1};
-      RowMapLinesOff vrows{pl, rs, g.zlo, Z - nvz, l0};
-      ct_lines<Y, false, kTeam, kEmax, TM>(max(0, min(kLinesTeam, nvz - l0)), twy, srows, vrows, vrows, false, true);
-    }
-    __syncthreads();                         // staging read; every valid row transformed
-    if (q + (int)gridDim.x < nplanes) pass2_stage_in<Y, Z, NT>(p, re2, q + gridDim.x, stg);
-    // z: the team's columns -- forward (the zero band read as zeros), product, inverse
-    {
-      const int kx = q % g.nx, f = (q / g.nx) % p.nfield;
-      const long long spec_off = (long long)kx * plane + l0;
-      const float2* spec = (f == p.nfield - 1 ? p.s2 : p.s1) + spec_off;
-      SmemLines tcols{pl + l0, 1, rs};
-      ct_fwd_mul_inv<Z, kTeam, kEmax, TM>(kLinesTeam, twz, tcols, SpectrumOperand{spec, Y, p.spec_len - spec_off},
-                                          BandCols{pl + l0, rs, g.zlo, Z - (nvz - g.zlo - 1)}, true);
-    }
-    __syncthreads();                         // every column transformed
-    // inverse y: the team's rows, the last stage straight to the buffer
-    {
-      const long long goff = (long long)q * plane + (long long)l0 * Y;
-      SmemLines trows{pl + l0 * rs, rs, 1};
-      ct_head_inplace<Y, true, kTeam, kEmax, 0, TM>(kLinesTeam, twy, trows);
-      ct_last_stage_out<Y, true, kTeam, TM>(kLinesTeam, tly, trows, GlobalRows{p.buf + goff, Y, p.buf_len - goff});
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
 // Pass 2 (fast, clustered): the plane of one (pair, field, kx) shared by a
 // cluster of CS blocks, for planes larger than one block's shared memory.
 // Every exchange is a push: the last stage of a transform stores its outputs
@@ -919,18 +821,9 @@ struct FastSize {
       }
     }
     // (planes beyond one block take the split path for the target spectra)
-    if constexpr (kPersist) {
-      if (p.mode == 0 && p.persist > 0 && pass2_pst_smem<N, N>(p.g.nvz) <= p.smem_max) {
-        const int nplanes = (int)(grid.x * grid.y * grid.z);
-        const int blocks = std::min(nplanes, p.persist);
-        k_pass2_pst<N, N><<<blocks, PlaneLaunch<N, N>::kThreads, pass2_pst_smem<N, N>(p.g.nvz), s>>>(p, re2, nplanes);
-        return;
-      }
-    }
     if constexpr (plane_fits_block<N>()) k_pass2_ct<N, N><<<grid, PlaneLaunch<N, N>::kThreads, smem, s>>>(p, re2);
   }
-  // the persistent plane pass: one block per SM (the 128^2 plane with its staging area)
-  static constexpr bool kPersist = PF_P2_PERSIST && N == 128;
+
   // compile-time tile rows where a tile of that many rows fits the block
   static constexpr bool kTy16 = PF_P3_CT_TY && 16 * N <= kMaxVoxPass3Fast;
   static constexpr bool kTy8 = PF_P3_CT_TY && 8 * N <= kMaxVoxPass3Fast;
@@ -964,9 +857,7 @@ struct FastSize {
     if constexpr (plane_fits_block<N>()) {
       if (e == cudaSuccess) e = allow_smem(k_pass2_ct<N, N>, smem_plane);
     }
-    if constexpr (kPersist) {
-      if (e == cudaSuccess) e = allow_smem(k_pass2_pst<N, N>, smem_plane);
-    }
+
     constexpr int CS = ClusterOf<N>::kCS;
     if constexpr (CS > 0) {
       if (e == cudaSuccess) e = allow_smem(k_pass2_cl<N, N, CS>, ClusterPlane<N, N, CS>::smem(N));

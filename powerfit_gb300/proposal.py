@@ -11,9 +11,10 @@ proposal path instead
    (``PF_FLAG_ROT_MAX``);
 2. builds per-rotation features from those coarse scores: the rotation's own
    score and its nearest rotations' scores in SO(3), z-scored over the map,
-   and how well the voxels holding the neighbours' maxima agree with the
+   how well the voxels holding the neighbours' maxima agree with the
    rotation's own (a true fit puts neighbouring rotations' peaks at one
-   place, noise scatters them);
+   place, noise scatters them), and how many of the map's top rotations put
+   their peak where this rotation puts its own (peak-position votes);
 3. scores the features with a small network (bfloat16 weights, float32
    accumulation; forward, gradient and Adam are this project's CUDA kernels,
    ``csrc/pf_learn.cu``), trained on pairs of coarse features and
@@ -37,8 +38,10 @@ from . import _lib
 
 COARSE_EDGE = 32
 NEIGHBOURS = 12
-FEATURES = 1 + NEIGHBOURS + 4      # own score, neighbour scores (descending), their mean and std,
-                                   # peak agreement and the agreement-weighted neighbour score
+BASE_FEATURES = 1 + NEIGHBOURS + 4  # own score, neighbour scores (descending), their mean and std,
+                                    # peak agreement and the agreement-weighted neighbour score
+FEATURES = BASE_FEATURES + 2        # and the peak-position votes (count and score-weighted)
+VOTE_TOP = 0.02                     # the map's top 2% of rotations (coarse score) cast the votes
 AGREE_SIGMA = 1.0                  # coarse voxels
 HIDDEN = 32
 TOP_FRACTION = 0.05
@@ -142,6 +145,20 @@ def coarsen(target, template, mask, voxelspacing, resolution, edge=COARSE_EDGE):
 # one map prepared for both searches
 # ---------------------------------------------------------------------------
 
+# batch and tile shapes chosen by the autotuner, per (grid shape, set size):
+# a run over many maps of one size tunes each search once
+_TUNING = {}
+
+
+def _tuned(ctx, shape, nrot, trial):
+    key = (tuple(shape), int(nrot))
+    if key in _TUNING:
+        ctx.set_tuning(**_TUNING[key])
+    else:
+        cfg = ctx.autotune(trial)
+        _TUNING[key] = {k: cfg[k] for k in ("pairs", "rows1", "rows3")}
+
+
 class SearchPair:
     """A map's fine and coarse searches (contexts on one device) over one rotation set."""
 
@@ -157,10 +174,10 @@ class SearchPair:
         self.fine = self._context(BaseCorrelator, target, template, mask, laplace, device)
         self.coarse = self._context(BaseCorrelator, ct, ctm, cm, laplace, device)
         self.coarse.set_rotations(self.rotmats)
-        # batch and tile shapes for both grids (short timed trial scans)
-        self.coarse.autotune(min(2048, self.nrot))
+        # batch and tile shapes for both grids (short timed trial scans, once per grid shape)
+        _tuned(self.coarse, cm.shape, self.nrot, min(2048, self.nrot))
         self.fine.set_rotations(self.rotmats[:min(512, self.nrot)])
-        self.fine.autotune(min(512, self.nrot))
+        _tuned(self.fine, np.asarray(target).shape, self.nrot, min(512, self.nrot))
 
     @staticmethod
     def _context(Base, target, template, mask, laplace, device):
@@ -208,9 +225,31 @@ class SearchPair:
 # features and the network
 # ---------------------------------------------------------------------------
 
-def features(coarse, nbr, shape, device=0):
+def peak_votes(z, v, shape):
+    """Peak-position votes of every rotation: how many of the map's top
+    rotations (coarse z-score in the top VOTE_TOP) hold their best coarse LCC
+    within one coarse voxel (periodic) of this rotation's own peak voxel, as
+    log(1 + count) and as the sum of those rotations' z-scores.  A copy of
+    the template in the map draws the peaks of many rotations near the true
+    one to its position; noise scatters them."""
+    import torch
+    nz, ny, nx = shape
+    n = nz * ny * nx
+    top = z >= torch.quantile(z, 1.0 - VOTE_TOP)
+    cnt = torch.bincount(v[top], minlength=n).float().reshape(1, 1, nz, ny, nx)
+    wsum = torch.bincount(v[top], weights=z[top], minlength=n).float().reshape(1, 1, nz, ny, nx)
+    grid = torch.cat([cnt, wsum], dim=1)
+    # 3x3x3 periodic box sum
+    box = sum(torch.roll(grid, (a, b, c), dims=(2, 3, 4)) for a in (-1, 0, 1) for b in (-1, 0, 1) for c in (-1, 0, 1))
+    flat = box.reshape(2, n)
+    return torch.log1p(flat[0][v]), flat[1][v]
+
+
+def features(coarse, nbr, shape, device=0, votes=True):
     """(R, FEATURES) float32 CUDA tensor from the coarse search's per-rotation
-    (best LCC, voxel) and the neighbour table (R, k); `shape` is the coarse grid."""
+    (best LCC, voxel) and the neighbour table (R, k); `shape` is the coarse
+    grid.  ``votes=False`` leaves out the two vote features (BASE_FEATURES
+    columns, the input of networks trained without them)."""
     import torch
     scores, voxels = coarse
     dev = "cuda:%d" % device
@@ -231,8 +270,12 @@ def features(coarse, nbr, shape, device=0):
     d = torch.minimum(d, ext - d)
     agree = torch.exp(-(d * d).sum(-1) / (2.0 * AGREE_SIGMA ** 2))
     wz = (agree * ns).sum(1, keepdim=True) / (agree.sum(1, keepdim=True) + 1e-6)
-    return torch.cat([z[:, None], srt, ns.mean(1, keepdim=True), ns.std(1, keepdim=True),
-                      agree.mean(1, keepdim=True), wz], dim=1).contiguous()
+    cols = [z[:, None], srt, ns.mean(1, keepdim=True), ns.std(1, keepdim=True), agree.mean(1, keepdim=True), wz]
+    if votes:
+        vc, vw = peak_votes(z, v, shape)
+        zs = lambda a: ((a - a.mean()) / (a.std() + 1e-12))[:, None]
+        cols += [zs(vc), zs(vw)]
+    return torch.cat(cols, dim=1).contiguous()
 
 
 def targets(fine_scores, device=0):
@@ -338,7 +381,7 @@ def rank_scores(net, coarse, nbr, shape, device=0):
     if net is None:
         import torch
         return torch.as_tensor(np.asarray(coarse[0], dtype=np.float32), device="cuda:%d" % device)
-    return net.forward(features(coarse, nbr, shape, device))
+    return net.forward(features(coarse, nbr, shape, device, votes=net.nin > BASE_FEATURES))
 
 
 def select(score, fraction=TOP_FRACTION):

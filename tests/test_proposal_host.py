@@ -134,3 +134,29 @@ def test_case_parameters_are_seeded_and_in_range():
         p = T.case_params(seed, 96)
         assert 1000 <= p["natoms"] <= 8000 and 5.0 <= p["resolution"] <= 9.0 and 1.0 <= p["snr"] <= 6.0
         assert 1 <= p["ncopies"] <= 3 and 1.2 <= p["voxelspacing"] <= 3.0
+
+
+def test_operating_fraction_is_the_smallest_that_keeps_validation_recall():
+    from powerfit_gb300 import proposal_train as T
+    # every map must rank its best fit inside half of the fraction
+    assert T.choose_fraction([0, 1, 2], 1000) == 0.005          # 2 < 0.005 * 1000 / 2
+    assert T.choose_fraction([0, 1, 9], 1000) == 0.02           # 9 < 10
+    assert T.choose_fraction([0, 300], 1000) == 1.0             # no candidate: the exhaustive search
+
+
+def test_peak_votes_count_the_top_rotations_peaking_nearby():
+    torch = pytest.importorskip("torch")
+    from powerfit_gb300 import proposal as PR
+    shape = (8, 8, 8)
+    n = 1000
+    g = torch.Generator().manual_seed(0)
+    z = torch.randn(n, generator=g)
+    v = torch.randint(0, 512, (n,), generator=g)
+    top = torch.argsort(z, descending=True)[:20]                # the top 2% cast votes
+    v[top] = 7 * 64 + 3 * 8 + 5                                 # all peak at voxel (7, 3, 5)
+    v[0] = 0 * 64 + 3 * 8 + 5                                   # one voxel away across the periodic z edge
+    v[1] = 3 * 64 + 3 * 8 + 1                                   # far away
+    cnt, wsum = PR.peak_votes(z, v, shape)
+    hits = int((v[top] == 7 * 64 + 3 * 8 + 5).sum())
+    assert abs(float(cnt[top[0]]) - np.log1p(hits)) < 1e-5 and float(cnt[0]) >= float(np.log1p(hits - 2))
+    assert float(cnt[1]) < 1.0 and float(wsum[top[0]]) > float(wsum[1])
