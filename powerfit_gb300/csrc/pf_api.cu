@@ -1,4 +1,5 @@
 // C ABI of the GB300 LCC search: context, device memory, launches.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -143,6 +144,12 @@ struct pf_ctx {
     cudaEvent_t a, b;
   };
   std::vector<Pending> pending;      // profiled launches whose events are not read yet
+  CUtensorMap tmap3{};               // fast pass 3: the tiles of buf as a 5-D tensor (TMA copies)
+  float2* tmap3_buf = nullptr;       // the buffer, pairs and tile rows the map was encoded for
+  long long tmap3_pairs = 0;
+  int tmap3_ty = 0;
+  bool tmap3_ok = false;
+  int* d_err = nullptr;              // device word: a tile copy's wait ran out (read by the synchronising calls)
   char err[512] = "";
 };
 
@@ -253,6 +260,74 @@ int ensure_part(pf_ctx* c) {
 long long buf_extent(const pf_ctx* c) {
   const long long n = c->buf ? c->buf_pairs * 3 * c->N : 0;
   return c->debug_buf_extent >= 0 && c->debug_buf_extent < n ? c->debug_buf_extent : n;
+}
+
+// 1 (default): pass-3 tiles by TMA tensor copies where a tensor map can
+// describe them; 0: always cp.async
+#ifndef PF_P3_TMA
+#define PF_P3_TMA 1
+#endif
+
+// cuTensorMapEncodeTiled from the driver (through the runtime: no link to
+// the driver library), or null where it is not available
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)ptr;
+  });
+  return fn;
+}
+
+// The tensor map of the pass-3 tiles for tile rows `ty`: buf as (y, z, kx,
+// field, pair) complex64 elements (8-byte words), box (ty, 1, nx, 3, 1);
+// encoded again when the buffer, its pairs or the tile rows change.  False
+// where TMA cannot take the tiles (edges beyond a box, row strides that are
+// not multiples of 16 bytes, a shrunk buffer extent): pass 3 then copies
+// with cp.async.
+bool ensure_tile_map(pf_ctx* c, int ty) {
+  if (c->tmap3_ok && c->tmap3_buf == c->buf && c->tmap3_pairs == c->buf_pairs && c->tmap3_ty == ty) return true;
+  c->tmap3_ok = false;
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || !c->buf || c->nx > 256 || ty > 256 || ty < 2 || (c->ny * sizeof(float2)) % 16 ||
+      (ty * sizeof(float2)) % 16 || c->debug_buf_extent >= 0)
+    return false;
+  const cuuint64_t e = sizeof(float2);
+  const cuuint64_t dims[5] = {(cuuint64_t)c->ny, (cuuint64_t)c->nz, (cuuint64_t)c->nx, 3, (cuuint64_t)c->buf_pairs};
+  const cuuint64_t strides[4] = {c->ny * e, (cuuint64_t)c->nz * c->ny * e, (cuuint64_t)c->nx * c->nz * c->ny * e,
+                                 3ull * c->nx * c->nz * c->ny * e};
+  const cuuint32_t box[5] = {(cuuint32_t)ty, 1, (cuuint32_t)c->nx, 3, 1};
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  if (fn(&c->tmap3, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5, c->buf, dims, strides, box, estr,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  c->tmap3_buf = c->buf;
+  c->tmap3_pairs = c->buf_pairs;
+  c->tmap3_ty = ty;
+  c->tmap3_ok = true;
+  return true;
+}
+
+// a tile copy of pass 3 whose wait ran out since the last check (clears the word)
+int check_tile_error(pf_ctx* c) {
+  if (!c->d_err) return PF_OK;
+  int e = 0;
+  PF_CUDA(c, cudaMemcpyAsync(&e, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  PF_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (e) {
+    PF_CUDA(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+    return fail(c, PF_E_CUDA, "a pass-3 tile copy did not complete within its time limit");
+  }
+  return PF_OK;
 }
 
 int ensure_buf(pf_ctx* c, int pairs) {
@@ -560,6 +635,8 @@ pf_ctx* pf_create(int nz, int ny, int nx, int device, int* status) {
   if (!rc) rc = alloc(c, (void**)&c->lcc, N * sizeof(float));
   if (!rc) rc = alloc(c, (void**)&c->rot, N * sizeof(int));
   if (!rc) rc = ensure_buf(c, c->pairs);
+  if (!rc) rc = alloc(c, (void**)&c->d_err, sizeof(int));
+  if (!rc && cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) rc = fail(c, PF_E_CUDA, "memset failed");
   if (!rc) {
     auto tx = twiddles(nx), ty = twiddles(ny), tz = twiddles(nz);
     if (cudaMemcpy(c->twx, tx.data(), nx * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -590,7 +667,7 @@ int pf_destroy(pf_ctx* c) {
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   c->own_stream = nullptr;
   void* ptrs[] = {c->twx, c->twy, c->twz, c->tmpl, c->mask, c->lcc_mask, c->spec, c->lcc, c->rot, c->buf, c->rots, c->rotd,
-                  c->rows_reach, c->rows_full, c->tmpl_pairs, c->part_lcc, c->part_rot, c->rotmax};
+                  c->rows_reach, c->rows_full, c->tmpl_pairs, c->part_lcc, c->part_rot, c->rotmax, c->d_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete c;
@@ -890,7 +967,10 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     const size_t s3f = pass3_smem(c->nx, ty3, npairs > 1 ? 2 : 1);
     rc = timed_launch(c, 2, [&] {
       if (fast) {
-        c->fl.pass3(p3, g3, s3f, c->stream);
+        const bool tm = PF_P3_TMA && ensure_tile_map(c, ty3);
+        p3.tma = tm ? 1 : 0;
+        p3.err = c->d_err;
+        c->fl.pass3(p3, tm ? &c->tmap3 : nullptr, g3, s3f, c->stream);
         if (g3.z != 2) return 1;
         k_combine<<<(unsigned)std::min<long long>((c->N + 255) / 256, 4 * 1024), 256, 0, c->stream>>>(
             c->part_lcc, c->part_rot, 0, c->lcc, c->rot, c->N);
@@ -918,7 +998,7 @@ int pf_get_results(pf_ctx* c, float* out_lcc, int32_t* out_rot) {
   PF_CUDA(c, cudaMemcpyAsync(out_rot, c->rot, c->N * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   PF_CUDA(c, cudaStreamSynchronize(c->stream));
   if (c->profiling) collect_events(c);
-  return PF_OK;
+  return check_tile_error(c);
 }
 
 int pf_get_rotation_best(pf_ctx* c, float* value, int32_t* voxel, int64_t first, int64_t count) {
@@ -955,7 +1035,7 @@ int pf_synchronize(pf_ctx* c) {
   DeviceGuard guard(c->device);
   PF_CUDA(c, cudaStreamSynchronize(c->stream));
   if (c->profiling) collect_events(c);
-  return PF_OK;
+  return check_tile_error(c);
 }
 
 int pf_scan(pf_ctx* c, const double* rotmats, int64_t nrot, int64_t rot_offset, float* out_lcc, int32_t* out_rot,

@@ -533,6 +533,8 @@ struct Pass3Params {
   int* __restrict__ rot;       // running argmax
   int ty;
   int fp64;                    // 1: variance and LCC in float64
+  int tma = 0;                 // fast path: tiles by one TMA tensor copy (the tensor map is a kernel argument)
+  int* err = nullptr;          // set to 1 when a tile copy's wait runs out
   // fast path with gridDim.z == 2: blocks with blockIdx.z == 1 take the later
   // half of the pairs, starting from 0, and keep their best in these arrays
   // (merged into lcc / rot afterwards, the earlier half winning ties)

@@ -6,7 +6,9 @@
 // rotation, so pass 1 neither transforms nor stores it and pass 2 reads zeros
 // for it without touching memory.
 #pragma once
+#include <cuda.h>   // CUtensorMap (the pass-3 tile copies)
 #include <algorithm>
+#include <cstring>
 #include <cooperative_groups.h>
 #include "pf_fft_ct.cuh"
 #include "pf_kernels.cuh"
@@ -554,9 +556,43 @@ struct ClusterOf {
 // float2 slots holding the list of a tile's voxels inside the lcc mask (one 16-bit entry each)
 __host__ __device__ inline int pass3_list_slots(int X, int ty) { return (ty * X * 2 + 7) / 8; }
 
-// twiddles, the voxel list, nbuf tile buffers
+// twiddles, the voxel list, nbuf tile buffers (on a 128-byte boundary: 128 bytes of slack)
 __host__ __device__ inline size_t pass3_smem(int X, int ty, int nbuf) {
-  return ((size_t)X + pass3_list_slots(X, ty) + (size_t)nbuf * 3 * ty * X) * sizeof(float2);
+  return ((size_t)X + pass3_list_slots(X, ty) + (size_t)nbuf * 3 * ty * X) * sizeof(float2) + 128;
+}
+
+// Tile of pass 3 for pair `pair` by one TMA tensor copy: the buffer viewed as
+// a 5-D tensor (y, z, kx, field, pair), box (ty, 1, X, 3, 1) at (y0, z, 0, 0,
+// pair), lands in shared memory as [field][kx][row] -- the tile's layout --
+// with rows beyond the grid filled with zeros; it completes on `bar`.
+__device__ __forceinline__ void pass3_tile_tma(const CUtensorMap* map, float2* dst, unsigned long long* bar, int y0,
+                                               int z, int pair, unsigned int bytes) {
+  const unsigned int b = smem_u32(bar), d = smem_u32(dst);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
+      "[%7];" ::"r"(d),
+      "l"(map), "r"(y0), "r"(z), "r"(0), "r"(0), "r"(pair), "r"(b)
+      : "memory");
+}
+
+// Bounded wait for completion `parity` of a tile barrier (2 s on the global timer).
+__device__ __forceinline__ bool pass3_tile_wait(unsigned long long* bar, unsigned int parity) {
+  const unsigned int b = smem_u32(bar);
+  unsigned long long t0;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (;;) {
+    unsigned int done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(b), "r"(parity)
+        : "memory");
+    if (done) return true;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (t - t0 > 2000000000ull) return false;
+  }
 }
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -627,15 +663,28 @@ constexpr int kVoxPass3Ct = (kMaxVoxPass3Fast + kThreadsPass3Ct - 1) / kThreadsP
 // TY > 0: the tile rows as a compile-time constant (the launcher picks this
 // instantiation when p.ty == TY), so every tile index folds into constants;
 // TY == 0 reads them from p.ty.
+//
+// Tiles arrive by one TMA tensor copy each (p.tma, the normal build) or by
+// 16-byte cp.async copies (the bounds-checked build, whose checks cover every
+// copy, and contexts without a tensor map).
 template <int X, int TY>
-__global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct(const Pass3Params p) {
+__global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm)
+    k_pass3_ct(const Pass3Params p, const __grid_constant__ CUtensorMap tmap) {
   constexpr int NT = kThreadsPass3Ct, VPT = kVoxPass3Ct;
   extern __shared__ float2 sm[];
   const Geometry& g = p.g;
   const int ty = TY > 0 ? TY : p.ty;        // a power of two >= 2 on this path
   float2* tw = sm;
   unsigned short* s_list = reinterpret_cast<unsigned short*>(sm + X);
-  float2* fbuf0 = sm + X + pass3_list_slots(X, ty);
+  float2* fbuf0 = reinterpret_cast<float2*>(
+      (reinterpret_cast<unsigned long long>(sm + X + pass3_list_slots(X, ty)) + 127ull) & ~127ull);
+#ifdef PF_BOUNDS_CHECK
+  const bool tma = false;
+#else
+  const bool tma = p.tma != 0;
+#endif
+  __shared__ unsigned long long s_bar[2];   // tile barriers of the two buffers (TMA)
+  unsigned int phase = 0;                   // bit b: parity of buffer b's next completion
   const int sh = TY > 0 ? ct_log2(TY) : __ffs(ty) - 1;
   const int fbuf_stride = 3 * ty * X;
 
@@ -650,11 +699,21 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct
   const int pb = (gridDim.z == 1 || blockIdx.z == 0) ? 0 : half;
   const int pe = gridDim.z == 1 ? p.npairs : (blockIdx.z == 0 ? half : p.npairs);
 
+  const unsigned int tile_bytes = (unsigned int)(fbuf_stride * sizeof(float2));
   // start the first tile's copies before anything else
-  if (pb < pe)
-    pass3_prefetch<X, NT>(p.buf + (long long)pb * 3 * fstride, p.buf_len - (long long)pb * 3 * fstride, fbuf0, ty, y0,
-                          g.ny, g.nz, z);
-  cp_async_commit();
+  if (tma) {
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_bar[0])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_bar[1])) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      if (pb < pe) pass3_tile_tma(&tmap, fbuf0, &s_bar[0], y0, z, pb, tile_bytes);
+    }
+  } else {
+    if (pb < pe)
+      pass3_prefetch<X, NT>(p.buf + (long long)pb * 3 * fstride, p.buf_len - (long long)pb * 3 * fstride, fbuf0, ty,
+                            y0, g.ny, g.nz, z);
+    cp_async_commit();
+  }
   for (int i = threadIdx.x; i < X; i += NT) tw[i] = p.twx[i];
 
   // voxel v of the tile: row r = v & (ty-1), column x = v >> log2(ty).  The
@@ -724,16 +783,33 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct
   }
 
   for (int pair = pb; pair < pe; ++pair) {
-    float2* fld = fbuf0 + ((pair - pb) & 1) * fbuf_stride;
-    if (pair + 1 < pe) {
-      pass3_prefetch<X, NT>(p.buf + (long long)(pair + 1) * 3 * fstride, p.buf_len - (long long)(pair + 1) * 3 * fstride,
-                            fbuf0 + ((pair + 1 - pb) & 1) * fbuf_stride, ty, y0, g.ny, g.nz, z);
-      cp_async_commit();
-      cp_async_wait_group<1>();
+    const int b = (pair - pb) & 1;
+    float2* fld = fbuf0 + b * fbuf_stride;
+    if (tma) {
+      // the other buffer was last read before the barrier that ended the previous pair
+      if (pair + 1 < pe && threadIdx.x == 0)
+        pass3_tile_tma(&tmap, fbuf0 + (b ^ 1) * fbuf_stride, &s_bar[b ^ 1], y0, z, pair + 1, tile_bytes);
+      const bool ok = pass3_tile_wait(&s_bar[b], (phase >> b) & 1u);
+      phase ^= 1u << b;
+      if (__syncthreads_or(!ok)) {             // a tile did not arrive: record it, wait for the copy in flight, stop
+        if (threadIdx.x == 0) {
+          if (p.err) atomicExch(p.err, 1);
+          if (pair + 1 < pe) pass3_tile_wait(&s_bar[b ^ 1], (phase >> (b ^ 1)) & 1u);
+        }
+        break;
+      }
     } else {
-      cp_async_wait_group<0>();
+      if (pair + 1 < pe) {
+        pass3_prefetch<X, NT>(p.buf + (long long)(pair + 1) * 3 * fstride,
+                              p.buf_len - (long long)(pair + 1) * 3 * fstride, fbuf0 + (b ^ 1) * fbuf_stride, ty, y0,
+                              g.ny, g.nz, z);
+        cp_async_commit();
+        cp_async_wait_group<1>();
+      } else {
+        cp_async_wait_group<0>();
+      }
+      __syncthreads();
     }
-    __syncthreads();
     TileLines lines{fld, sh, ty, X * ty};
     ct_lines<X, true, NT, PF_PASS3_EMAX>(3 * ty, tw, lines, lines, lines, true, true);
     const long long ra = p.first_rot + 2LL * pair;
@@ -769,6 +845,8 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct
       }
     }
     if (p.rotmax) rotmax_block(p.rotmax, p.rotmax_len, ra, has_b, ka, kb, s_red);
+    // this tile buffer's generic reads and writes come before the next TMA copy into it
+    if (tma) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
   }
 #pragma unroll
@@ -789,7 +867,7 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm) k_pass3_ct
 struct FastLaunch {
   void (*pass1)(const Pass1Params&, int re2, dim3 grid, size_t smem, cudaStream_t s);
   void (*pass2)(const Pass2Params&, int re2, dim3 grid, size_t smem, cudaStream_t s);
-  void (*pass3)(const Pass3Params&, dim3 grid, size_t smem, cudaStream_t s);
+  void (*pass3)(const Pass3Params&, const CUtensorMap* map, dim3 grid, size_t smem, cudaStream_t s);
   cudaError_t (*set_attrs)(size_t smem_line, size_t smem_plane);
   bool cluster_plane;   // pass 2 (correlation) runs even where a plane exceeds one block's shared memory
 };
@@ -827,14 +905,18 @@ struct FastSize {
   // compile-time tile rows where a tile of that many rows fits the block
   static constexpr bool kTy16 = PF_P3_CT_TY && 16 * N <= kMaxVoxPass3Fast;
   static constexpr bool kTy8 = PF_P3_CT_TY && 8 * N <= kMaxVoxPass3Fast;
-  static void pass3(const Pass3Params& p, dim3 grid, size_t smem, cudaStream_t s) {
+  // `map`: the tensor map of the tiles (p.tma set), or null (cp.async copies)
+  static void pass3(const Pass3Params& p, const CUtensorMap* map, dim3 grid, size_t smem, cudaStream_t s) {
+    CUtensorMap none;
+    if (!map) std::memset(&none, 0, sizeof(none));
+    const CUtensorMap& m = map ? *map : none;
     if constexpr (kTy16) {
-      if (p.ty == 16) { k_pass3_ct<N, 16><<<grid, kThreadsPass3Ct, smem, s>>>(p); return; }
+      if (p.ty == 16) { k_pass3_ct<N, 16><<<grid, kThreadsPass3Ct, smem, s>>>(p, m); return; }
     }
     if constexpr (kTy8) {
-      if (p.ty == 8) { k_pass3_ct<N, 8><<<grid, kThreadsPass3Ct, smem, s>>>(p); return; }
+      if (p.ty == 8) { k_pass3_ct<N, 8><<<grid, kThreadsPass3Ct, smem, s>>>(p, m); return; }
     }
-    k_pass3_ct<N, 0><<<grid, kThreadsPass3Ct, smem, s>>>(p);
+    k_pass3_ct<N, 0><<<grid, kThreadsPass3Ct, smem, s>>>(p, m);
   }
   template <class K>
   static cudaError_t allow_smem(K kernel, size_t bytes) {
