@@ -225,6 +225,22 @@ class SearchPair:
 # features and the network
 # ---------------------------------------------------------------------------
 
+def zscore(a, rel=1e-6):
+    """(a - mean) / std, or zeros where `a` has no spread: a feature that is the
+    same for every rotation of a map (all peaks at one voxel, say) carries no
+    information, and dividing its rounding residue by a zero spread would
+    give inputs of 1e5 and more."""
+    import torch
+    m = a.mean()
+    sd = a.std()
+    if not bool(torch.isfinite(sd)) or float(sd) <= rel * max(1.0, abs(float(m))):
+        return torch.zeros_like(a)
+    return (a - m) / sd
+
+
+FEATURE_CLIP = 20.0   # features are clamped to +-20 (z-scores of a well-spread feature stay far inside)
+
+
 def peak_votes(z, v, shape):
     """Peak-position votes of every rotation: how many of the map's top
     rotations (coarse z-score in the top VOTE_TOP) hold their best coarse LCC
@@ -257,7 +273,7 @@ def features(coarse, nbr, shape, device=0, votes=True):
     finite = torch.isfinite(s)
     lo = s[finite].min() if bool(finite.any()) else torch.tensor(0.0, device=s.device)
     s = torch.where(finite, s, lo)
-    z = (s - s.mean()) / (s.std() + 1e-12)
+    z = zscore(s)
     nb = torch.as_tensor(nbr, device=dev)
     ns = z[nb]
     srt = torch.sort(ns, dim=1, descending=True).values
@@ -273,9 +289,10 @@ def features(coarse, nbr, shape, device=0, votes=True):
     cols = [z[:, None], srt, ns.mean(1, keepdim=True), ns.std(1, keepdim=True), agree.mean(1, keepdim=True), wz]
     if votes:
         vc, vw = peak_votes(z, v, shape)
-        zs = lambda a: ((a - a.mean()) / (a.std() + 1e-12))[:, None]
-        cols += [zs(vc), zs(vw)]
-    return torch.cat(cols, dim=1).contiguous()
+        cols += [zscore(vc)[:, None], zscore(vw)[:, None]]
+    x = torch.cat(cols, dim=1)
+    return torch.nan_to_num(x, nan=0.0, posinf=FEATURE_CLIP, neginf=-FEATURE_CLIP).clamp_(-FEATURE_CLIP,
+                                                                                       FEATURE_CLIP).contiguous()
 
 
 def targets(fine_scores, device=0):

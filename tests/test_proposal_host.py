@@ -160,3 +160,18 @@ def test_peak_votes_count_the_top_rotations_peaking_nearby():
     hits = int((v[top] == 7 * 64 + 3 * 8 + 5).sum())
     assert abs(float(cnt[top[0]]) - np.log1p(hits)) < 1e-5 and float(cnt[0]) >= float(np.log1p(hits - 2))
     assert float(cnt[1]) < 1.0 and float(wsum[top[0]]) > float(wsum[1])
+
+
+def test_zscore_of_a_constant_feature_is_zero():
+    """A vote feature that is the same for every rotation (every peak at one
+    voxel) must not turn its rounding residue into inputs of 1e5."""
+    torch = pytest.importorskip("torch")
+    from powerfit_gb300 import proposal as PR
+    a = torch.full((207576,), float(np.log1p(4151.0)), dtype=torch.float32)
+    assert torch.count_nonzero(PR.zscore(a)) == 0
+    z = torch.randn(1000, generator=torch.Generator().manual_seed(1))
+    v = torch.full((1000,), 77, dtype=torch.int64)           # every rotation peaks at one voxel
+    cnt, wsum = PR.peak_votes(z, v, (8, 8, 8))
+    assert torch.count_nonzero(PR.zscore(cnt)) == 0
+    b = PR.zscore(z)
+    assert abs(float(b.mean())) < 1e-5 and abs(float(b.std()) - 1.0) < 1e-4
