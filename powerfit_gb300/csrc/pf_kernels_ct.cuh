@@ -618,31 +618,6 @@ struct TileLines {
   }
 };
 
-// The tile's lines from line l0 on (a team's share of the inverse x transform)
-struct TileLinesOff {
-  float2* base;
-  int sh, ty, xty, l0;
-  __device__ __forceinline__ int off(int line) const {
-    const int l = l0 + line;
-    return (l >> sh) * xty + (l & (ty - 1));
-  }
-  __device__ __forceinline__ float2 load(int line, int idx) const {
-    const float2* q = base + off(line) + idx * ty;
-    return PF_CHECK_SMEM(kChkSmem, q, 8) ? *q : make_float2(0.f, 0.f);
-  }
-  __device__ __forceinline__ void store(int line, int idx, float2 v) const {
-    float2* q = base + off(line) + idx * ty;
-    if (PF_CHECK_SMEM(kChkSmem, q, 8)) *q = v;
-  }
-};
-
-// 1 (default): the inverse x transform of a pass-3 tile in two teams of half
-// the block, each over half of the tile's 3 * ty lines on its own barrier;
-// 0: block-wide stages
-#ifndef PF_P3_TEAMS
-#define PF_P3_TEAMS 1
-#endif
-
 template <int X, int NT>
 __device__ __forceinline__ void pass3_prefetch(const float2* __restrict__ base, long long lim, float2* fld, int ty,
                                                int y0, int ny, int nz, int z) {
@@ -835,18 +810,8 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm)
       }
       __syncthreads();
     }
-#if PF_P3_TEAMS
-    {
-      using TM = GroupTeam<NT / 2>;
-      const int nl = (3 * ty) >> 1;           // ty is even on this path
-      TileLinesOff lines{fld, sh, ty, X * ty, TM::team() * nl};
-      ct_lines<X, true, NT / 2, PF_PASS3_EMAX, TM>(nl, tw, lines, lines, lines, true, true);
-      __syncthreads();                        // all three fields of every voxel transformed
-    }
-#else
     TileLines lines{fld, sh, ty, X * ty};
     ct_lines<X, true, NT, PF_PASS3_EMAX>(3 * ty, tw, lines, lines, lines, true, true);
-#endif
     const long long ra = p.first_rot + 2LL * pair;
     const bool has_b = ra + 1 < p.nrot;
     unsigned long long ka = 0, kb = 0;
