@@ -19,7 +19,9 @@ proposal path instead
    accumulation; forward, gradient and Adam are this project's CUDA kernels,
    ``csrc/pf_learn.cu``), trained on pairs of coarse features and
    full-resolution per-rotation best LCC that the exhaustive search generates;
-4. searches the top fraction (5%) of the rotations at full resolution.
+4. searches the top fraction of the rotations at full resolution: the
+   operating fraction chosen on validation maps when the network was trained
+   and stored with its weights (0.2% for the shipped network).
 
 The exhaustive search stays the fallback (``fraction=1``) and the measure of
 the proposal: recall is whether the proposal's rotations contain the
@@ -339,6 +341,7 @@ class ProposalNet:
         self.grad = torch.zeros_like(self.p)
         self.loss = torch.zeros(1, dtype=torch.float32, device=dev)
         self.step = 0
+        self.fraction = TOP_FRACTION     # operating fraction of the proposal search
 
     def _stream(self):
         import torch
@@ -384,8 +387,16 @@ class ProposalNet:
 
     @classmethod
     def load(cls, path, device=0):
-        d = np.load(path)
-        return cls(int(d["nin"]), int(d["nh"]), device=device, params=d["params"])
+        """Weights saved by `save`; ``fraction`` is the operating fraction
+        stored with them (chosen on validation maps when the network was
+        trained), else TOP_FRACTION."""
+        import ast
+        with np.load(path) as d:
+            net = cls(int(d["nin"]), int(d["nh"]), device=device, params=d["params"])
+            meta = ast.literal_eval(str(d["meta"])) if "meta" in d.files else {}
+        fr = meta.get("fractions") if isinstance(meta, dict) else None
+        net.fraction = float(fr["network"]) if fr and "network" in fr else TOP_FRACTION
+        return net
 
 
 # ---------------------------------------------------------------------------
@@ -409,10 +420,14 @@ def select(score, fraction=TOP_FRACTION):
     return torch.sort(torch.topk(s, k).indices).values.cpu().numpy()
 
 
-def proposal_search(pair, net, nbr, fraction=TOP_FRACTION, timings=None):
-    """Coarse search, ranking, full-resolution search of the top fraction.
+def proposal_search(pair, net, nbr, fraction=None, timings=None):
+    """Coarse search, ranking, full-resolution search of the top fraction
+    (default: the network's operating fraction, or TOP_FRACTION for the coarse
+    score alone, ``net`` None; 1 is the exhaustive search).
     Returns (lcc, rot, selected rotation indices)."""
     import torch
+    if fraction is None:
+        fraction = net.fraction if net is not None else TOP_FRACTION
     t0 = time.perf_counter()
     coarse = pair.coarse_scores()
     t1 = time.perf_counter()

@@ -12,7 +12,7 @@ without the network), each at its own operating fraction -- and the script
 reports best-fit recall and time to best fit.  The seeded maps are built in
 worker processes while the GPU searches.
 
-    python -m powerfit_gb300.proposal_train --maps 240 --valid 24 --eval 100 \\
+    python -m powerfit_gb300.proposal_train --maps 200 --valid 24 --eval 100 --workers 12 \\
         --out powerfit_gb300/data/proposal_net.npz --report powerfit_gb300/data/proposal_net_report.json
 """
 from __future__ import annotations

@@ -175,3 +175,22 @@ def test_zscore_of_a_constant_feature_is_zero():
     assert torch.count_nonzero(PR.zscore(cnt)) == 0
     b = PR.zscore(z)
     assert abs(float(b.mean())) < 1e-5 and abs(float(b.std()) - 1.0) < 1e-4
+
+
+def test_shipped_network_report_meets_the_recall_and_time_targets():
+    """The committed held-out evaluation of the shipped weights: at the
+    operating fraction stored with them, the network finds at least 99% of
+    the exhaustive best fits in at most 0.25x the exhaustive time, and finds
+    at least as many as the coarse score alone at the same fraction."""
+    import json
+    from powerfit_gb300 import proposal as PR, proposal_train as T
+    fr = T.operating_fractions(PR.default_weights())
+    report = PR.default_weights().replace("proposal_net.npz", "proposal_net_report.json")
+    with open(report) as f:
+        rep = json.load(f)
+    s, rows = rep["summary"], rep["rows"]
+    assert len(rows) >= 100 and s["fractions"] == fr
+    assert all(r["network"]["fraction"] == fr["network"] for r in rows)
+    assert s["network"]["recall"] >= 0.99 and s["network"]["time_vs_exhaustive"] <= 0.25
+    assert s["network"]["recall"] >= s["coarse_only"]["recall"]
+    assert s == {**s, **T.summarise(rows)}
