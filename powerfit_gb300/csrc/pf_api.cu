@@ -112,8 +112,9 @@ struct pf_ctx {
   float2* spec = nullptr;          // [2][kx][kz][ky]
   float* lcc = nullptr;
   int* rot = nullptr;
-  float* part_lcc = nullptr;        // fast pass 3 split over two blocks per tile: best of the later pairs
+  float* part_lcc = nullptr;        // fast pass 3 split over several blocks per tile: best of the later parts
   int* part_rot = nullptr;
+  int part_cap = 0;                  // part arrays of N voxels held in part_lcc / part_rot
   unsigned long long* rotmax = nullptr;   // PF_FLAG_ROT_MAX: per-rotation (best LCC, voxel) keys
   long long rotmax_cap = 0;
   float2* buf = nullptr;
@@ -244,15 +245,21 @@ void choose_tiles(pf_ctx* c) {
   c->pairs = (int)std::max(1LL, std::min(16LL, p));
 }
 
-// best of the later half of a batch's pairs (fast pass 3 split over two
-// blocks per tile); zero outside the lcc mask, which no block writes
-int ensure_part(pf_ctx* c) {
-  if (c->part_lcc) return PF_OK;
-  int rc = alloc(c, (void**)&c->part_lcc, c->N * sizeof(float));
-  if (!rc) rc = alloc(c, (void**)&c->part_rot, c->N * sizeof(int));
+// best of the later parts of a batch's pairs (fast pass 3 split over several
+// blocks per tile): kPass3MaxParts - 1 arrays of N voxels, allocated at the
+// first split (so that no later scan allocates, or waits, again); zero
+// outside the lcc mask, which no block writes
+int ensure_part(pf_ctx* c, int nparts) {
+  if (c->part_cap >= nparts) return PF_OK;
+  if (c->part_lcc) return fail(c, PF_E_ARG, "pass 3: %d part arrays asked, %d held", nparts, c->part_cap);
+  const int cap = kPass3MaxParts - 1;
+  const size_t n = (size_t)cap * c->N;
+  int rc = alloc(c, (void**)&c->part_lcc, n * sizeof(float));
+  if (!rc) rc = alloc(c, (void**)&c->part_rot, n * sizeof(int));
   if (rc) return rc;
-  PF_CUDA(c, cudaMemsetAsync(c->part_lcc, 0, c->N * sizeof(float), c->stream));
-  PF_CUDA(c, cudaMemsetAsync(c->part_rot, 0, c->N * sizeof(int), c->stream));
+  PF_CUDA(c, cudaMemsetAsync(c->part_lcc, 0, n * sizeof(float), c->stream));
+  PF_CUDA(c, cudaMemsetAsync(c->part_rot, 0, n * sizeof(int), c->stream));
+  c->part_cap = cap;
   return PF_OK;
 }
 
@@ -950,16 +957,21 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
     p3.buf_len = buf_extent(c);
     dim3 g3(c->nz, (c->ny + ty3 - 1) / ty3, 1);
     // Each pass-3 block runs through all pairs of the batch, so a grid of a
-    // few waves leaves much of its last wave idle; splitting the pairs over
-    // two blocks per tile (merged afterwards) evens the waves out.
+    // few waves (or of fewer tiles than the GPU holds blocks) leaves much of
+    // its last wave idle; splitting the pairs over up to kPass3MaxParts blocks
+    // per tile (merged afterwards) evens the waves out.  A split is taken only
+    // where it fills the waves by more than 5 points over the fewer parts.
     if (fast && npairs >= 4 && c->num_sms > 0) {
       const double slots = (double)kPass3BlocksPerSm * c->num_sms;
       auto eff = [&](double blocks) { const double w = blocks / slots; return w / std::ceil(w); };
       const double tiles = (double)g3.x * g3.y;
-      if (eff(2 * tiles) > eff(tiles) + 0.05) {
-        rc = ensure_part(c);
+      int parts = 1;
+      for (int k = 2; k <= kPass3MaxParts && 2 * k <= npairs; ++k)
+        if (eff(k * tiles) > eff(parts * tiles) + 0.05) parts = k;
+      if (parts > 1) {
+        rc = ensure_part(c, parts - 1);
         if (rc) return rc;
-        g3.z = 2;
+        g3.z = parts;
         p3.part_lcc = c->part_lcc;
         p3.part_rot = c->part_rot;
       }
@@ -971,9 +983,9 @@ int pf_scan_resident(pf_ctx* c, int64_t first, int64_t count, int64_t rot_offset
         p3.tma = tm ? 1 : 0;
         p3.err = c->d_err;
         c->fl.pass3(p3, tm ? &c->tmap3 : nullptr, g3, s3f, c->stream);
-        if (g3.z != 2) return 1;
-        k_combine<<<(unsigned)std::min<long long>((c->N + 255) / 256, 4 * 1024), 256, 0, c->stream>>>(
-            c->part_lcc, c->part_rot, 0, c->lcc, c->rot, c->N);
+        if (g3.z == 1) return 1;
+        k_combine_parts<<<(unsigned)std::min<long long>((c->N + 255) / 256, 4 * 1024), 256, 0, c->stream>>>(
+            c->part_lcc, c->part_rot, (int)g3.z - 1, c->lcc, c->rot, c->N);
         return 2;
       }
       if (tc) k_pass3<true><<<g3, kThreadsLine, s3, c->stream>>>(p3);

@@ -535,9 +535,10 @@ struct Pass3Params {
   int fp64;                    // 1: variance and LCC in float64
   int tma = 0;                 // fast path: tiles by one TMA tensor copy (the tensor map is a kernel argument)
   int* err = nullptr;          // set to 1 when a tile copy's wait runs out
-  // fast path with gridDim.z == 2: blocks with blockIdx.z == 1 take the later
-  // half of the pairs, starting from 0, and keep their best in these arrays
-  // (merged into lcc / rot afterwards, the earlier half winning ties)
+  // fast path with gridDim.z == P > 1: the batch's pairs split into P parts
+  // of ceil(npairs / P) in order; blocks with blockIdx.z == k > 0 take part k,
+  // starting from 0, and keep their best in these arrays at offset (k-1)*N
+  // (merged into lcc / rot afterwards in part order, earlier parts winning ties)
   float* __restrict__ part_lcc = nullptr;
   int* __restrict__ part_rot = nullptr;
   // with PF_FLAG_ROT_MAX: per rotation of the uploaded set, the best LCC over
@@ -637,6 +638,8 @@ constexpr int kMaxVoxPass3Fast = PF_PASS3_MAXVOX;
 #define PF_PASS3_MINB 2
 #endif
 constexpr int kPass3BlocksPerSm = PF_PASS3_MINB;
+// most blocks one tile's pairs are split over (fast pass 3)
+constexpr int kPass3MaxParts = 4;
 
 #ifdef PF_GENERIC_KERNELS
 template <bool TC>
@@ -843,6 +846,22 @@ __global__ void k_combine(const float* __restrict__ part_lcc, const int* __restr
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const float v = part_lcc[i];
     if (v > lcc[i]) { lcc[i] = v; rot[i] = (int)(part_rot[i] + rot_add); }
+  }
+}
+
+// merge of `nparts` part arrays (stride n) into lcc / rot, in part order:
+// the same as k_combine once per part, so earlier parts keep their ties
+__global__ void k_combine_parts(const float* __restrict__ part_lcc, const int* __restrict__ part_rot, int nparts,
+                                float* __restrict__ lcc, int* __restrict__ rot, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float best = lcc[i];
+    int r = 0;
+    bool won = false;
+    for (int k = 0; k < nparts; ++k) {
+      const float v = part_lcc[k * n + i];
+      if (v > best) { best = v; r = part_rot[k * n + i]; won = true; }
+    }
+    if (won) { lcc[i] = best; rot[i] = r; }
   }
 }
 

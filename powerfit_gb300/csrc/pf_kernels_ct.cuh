@@ -252,12 +252,15 @@ struct RowMapLinesOff {
 
 // Block shape of the plane pass: a plane of 128 x 128 or more fills one block
 // per SM (shared memory), which then runs 1024 threads; smaller planes run two
-// 512-thread blocks per SM.  Both leave 64 registers a thread.
+// 512-thread blocks per SM, and planes of at most 32 x 32 (whose stages hold
+// 128 to 256 butterflies) eight 128-thread blocks per SM, so that every
+// thread has a butterfly.  All leave 64 registers a thread.
 template <int Y, int Z>
 struct PlaneLaunch {
   static constexpr bool kBig = Y * Z >= 128 * 128;
-  static constexpr int kThreads = kBig ? 1024 : 512;
-  static constexpr int kMinBlocks = kBig ? 1 : 2;
+  static constexpr bool kSmall = Y * Z <= 32 * 32;
+  static constexpr int kThreads = kBig ? 1024 : (kSmall ? 128 : 512);
+  static constexpr int kMinBlocks = kBig ? 1 : (kSmall ? 8 : 2);
 };
 
 template <int Y, int Z>
@@ -694,10 +697,10 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm)
   const long long zoff = (long long)z * g.ny * X;
   const long long fstride = (long long)X * g.nz * g.ny;
 
-  // pairs of this block: all, or one half (blockIdx.z) when the pairs are split over two blocks
-  const int half = (p.npairs + 1) >> 1;
-  const int pb = (gridDim.z == 1 || blockIdx.z == 0) ? 0 : half;
-  const int pe = gridDim.z == 1 ? p.npairs : (blockIdx.z == 0 ? half : p.npairs);
+  // pairs of this block: all, or part blockIdx.z of gridDim.z when the pairs are split over several blocks
+  const int per = (p.npairs + (int)gridDim.z - 1) / (int)gridDim.z;
+  const int pb = min(p.npairs, (int)blockIdx.z * per);
+  const int pe = min(p.npairs, pb + per);
 
   const unsigned int tile_bytes = (unsigned int)(fbuf_stride * sizeof(float2));
   // start the first tile's copies before anything else
@@ -763,8 +766,9 @@ __global__ void __launch_bounds__(kThreadsPass3Ct, kPass3BlocksPerSm)
   }
   __syncthreads();
   const int total = s_warp[NT / 32];
-  float* __restrict__ out_lcc = blockIdx.z == 0 ? p.lcc : p.part_lcc;
-  int* __restrict__ out_rot = blockIdx.z == 0 ? p.rot : p.part_rot;
+  const long long part_off = blockIdx.z == 0 ? 0 : (long long)(blockIdx.z - 1) * g.nz * g.ny * X;
+  float* __restrict__ out_lcc = blockIdx.z == 0 ? p.lcc : p.part_lcc + part_off;
+  int* __restrict__ out_rot = blockIdx.z == 0 ? p.rot : p.part_rot + part_off;
   float best[VPT];
   int brot[VPT];
 #pragma unroll
