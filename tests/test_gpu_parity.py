@@ -211,6 +211,26 @@ def test_batching_pruning_and_accumulate_are_exact(lib):
     assert np.array_equal(r[upd], base.rot[upd] + 1000)
 
 
+def test_pass3_pair_parts_are_exact(lib):
+    """At 32^3 a pass-3 grid of 32 z planes x 2 tiles leaves most of the GPU
+    idle, so the batch's pairs are split over up to four blocks per tile and
+    merged in part order.  Every split (2, 3 and 4 parts, a last part left
+    empty, partial batches without a split) gives the unsplit result bit for
+    bit, and that result meets the oracle's parity criterion."""
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    target, template, mask = _synthetic((32, 32, 32), 3.0, 300, 8.0, 5, False)
+    rot = quat_to_rotmat(super_fibonacci(75))            # 38 pairs, the last half-empty
+    base = correlator(target, template, mask, rot, False, pairs=1, rows1=8, rows3=16)
+    ctx = base.context
+    for pairs in (4, 6, 9, 16, 38):
+        ctx.set_tuning(pairs=pairs, rows1=8, rows3=16)
+        lcc, r = ctx.scan(rot)
+        assert np.array_equal(lcc, base.lcc) and np.array_equal(r, base.rot), pairs
+    p = O.prepare(target, template, mask, False)
+    ref_lcc, ref_rot, ref_second = O.scan(p, rot, track_second=True)
+    check_parity(base.lcc, base.rot, ref_lcc, ref_rot, ref_second, "32^3 parts")
+
+
 def test_translation_equivariance(lib):
     from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
     target, template, mask = _synthetic((48, 48, 48), 2.5, 800, 8.0, 4, False)
