@@ -624,9 +624,11 @@ def run_precision(args):
     """Precision study: max |dLCC| and argmax agreement of the GPU variants
     against the float64 oracle, on a rotation subset of the configuration:
     float32 FFTs with float-float or float64 normalisation, and the DFT stages
-    on the tensor cores in split-bf16x3 (PF_FLAG_TENSOR_DFT; runtime-planned
-    kernels).  Each variant's search speed is timed on a larger slice, next to
-    the float32 runtime-planned kernels it replaces."""
+    on the tensor cores in split-bf16x3 (PF_FLAG_TENSOR_DFT with mma.sync;
+    runtime-planned kernels).  Each variant's search speed is timed on a larger slice, next to
+    the float32 runtime-planned kernels it replaces.  With
+    PF_FLAG_TENSOR_TC05 the plane pass's stages run on tcgen05; grids whose
+    plane does not fit one block's shared memory report it unsupported."""
     import multiprocessing as mp
     cores = os.cpu_count() or 1
     pool = mp.get_context("spawn").Pool(cores)
@@ -656,13 +658,19 @@ def run_precision(args):
     timed = rot[:min(rot.shape[0], args.precision_timed)]
     variants = (("fp32_fft+floatfloat_norm", 0), ("fp32_fft+fp64_norm", _lib.PF_FLAG_FP64_NORM),
                 ("fp32_fft_runtime_planned+floatfloat_norm", _lib.PF_FLAG_GENERIC),
-                ("bf16x3_tensor_dft+floatfloat_norm", _lib.PF_FLAG_TENSOR_DFT))
+                ("bf16x3_tensor_dft+floatfloat_norm", _lib.PF_FLAG_TENSOR_DFT),
+                ("bf16x3_tensor_dft_tcgen05_plane+floatfloat_norm",
+                 _lib.PF_FLAG_TENSOR_DFT | _lib.PF_FLAG_TENSOR_TC05))
     for name, flags in variants:
         corr = CUDACorrelator(target, laplace=cfg["laplace"], flags=flags)
         corr.template = template
         corr.mask = mask
         corr.rotations = sub
-        corr.scan()
+        try:
+            corr.scan()
+        except _lib.PowerFitError as e:        # a variant this grid does not support
+            res[name] = {"unsupported": str(e)}
+            continue
         fin = np.isfinite(lcc)
         err = float(np.max(np.abs(corr.lcc[fin] - lcc[fin])))
         clear = fin & ((lcc - second) > 1e-4) & (lcc > 0)
@@ -697,7 +705,8 @@ def run_kernels(args):
     runtime-planned search passes and target spectra (PF_FLAG_GENERIC), the
     same passes with the DFT stages on the tensor cores (PF_FLAG_TENSOR_DFT:
     mma.sync; with PF_FLAG_TENSOR_TC05 the plane pass's stages on tcgen05),
-    the float64 unit mirrors, the shard merge and the proposal network's kernels.
+    the float64 unit mirrors, the shard merge, the proposal network's kernels
+    and the learned proposal's coarse 32^3 search (2,048 rotations).
     Wall time per call (synchronised); meant as the command an ncu capture
     of these kernels runs."""
     import torch
@@ -758,6 +767,22 @@ def run_kernels(args):
     timed("mlp forward", lambda: net.forward(x))
     timed("mlp grad", lambda: _lib.mlp_grad(x, t, w, net.nin, net.nh, net.pb, 1.0 / rows, net.grad, net.loss))
     timed("mlp adam", lambda: _lib.mlp_adam(net.p, net.pb, net.grad, net.m, net.v, 1e-3, 1))
+    # the learned proposal's coarse search: the map brought to 32^3, 2,048
+    # rotations with per-rotation maxima (the 32^3 fast kernels: 128-thread
+    # plane-pass blocks, pass 3 split over four pair parts per tile and merged
+    # by k_combine_parts)
+    ct, ctm, cm, _, _ = PR.coarsen(target, template, mask, case.voxelspacing, case.resolution)
+    cb = BaseCorrelator(ct)
+    cb.template = ctm
+    cb.mask = cm
+    cctx = _lib.Context(ct.shape)
+    cctx.set_target(cb._target, cb._lcc_mask)
+    cctx.set_template_mask(cb._template, cb._mask, float(cb._norm_factor), cb._rmax)
+    cctx.set_tuning(pairs=128, rows1=32, rows3=16)
+    cctx.set_rotations(quat_to_rotmat(super_fibonacci(2048)))
+    timed("coarse 32^3 search (2,048 rotations)",
+          lambda: (cctx.scan_resident(0, 2048, 0, _lib.PF_FLAG_ROT_MAX), cctx.synchronize()))
+    cctx.close()
     print(json.dumps({"metric": "per-call wall time of the auxiliary kernels (128^3)", "unit": "s",
                       "values": times, "config": {"workload": "kernels", "grid": list(target.shape)}}), flush=True)
     return 0
