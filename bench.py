@@ -224,9 +224,10 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(r["wall_s"] for r in runs) / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded map, template, mask; %s)" % desc,
-        "config": {"workload": args.config, "grid": list(target.shape), "laplace": cfg["laplace"],
-                   "core_weighted": cfg["core_weighted"], "rotation_set_size": int(rot.shape[0]),
-                   "sample_rotations_per_step": cores * per_core},
+        "config": {"workload": args.config, "grid": list(target.shape), "voxelspacing": cfg["voxelspacing"],
+                   "laplace": cfg["laplace"], "core_weighted": cfg["core_weighted"],
+                   "rotation_set_size": int(rot.shape[0]), "rotations_per_step": cores * per_core,
+                   "l2": "not applicable (host cores)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": "%d rotations per step (%d per core) from %s, _cpu_scan structure, numpy.fft; "
                                    "rate over the rotation loops (the per-process set-up, once per process in a "
@@ -471,9 +472,11 @@ def run_ours(args, rank, world, local_rank):
         "config": {"workload": args.config, "grid": list(shape), "voxelspacing": cfg["voxelspacing"],
                    "laplace": cfg["laplace"], "core_weighted": cfg["core_weighted"],
                    "rotation_set_size": nset, "rotations_per_step": per_step,
-                   "pairs_per_batch": pairs, "rows_pass1": ty1, "rows_pass3": ty3, "tuning": tuned,
+                   "l2": "flushed (256 MiB write) before every timed step"},
+        # the search's own shapes (the reference arm has none): batch and
+        # tiles from the autotuner, and the pruning geometry of this template
+        "search": {"pairs_per_batch": pairs, "rows_pass1": ty1, "rows_pass3": ty3, "tuning": tuned,
                    "reach_radius": re, "planes": geo["valid_planes"], "disk_rows": disk,
-                   "l2": "flushed (256 MiB write) before every timed step",
                    "full_search_s": nset / (value / world)},
         "clocks": clk,
         "wall_s": wall,
