@@ -83,6 +83,15 @@ def workload(name, nrot_override=0):
     return cfg, case.target.astype(np.float64), case.template, mask, rot, desc
 
 
+def workload_config(name, cfg, shape, nset, per_step, l2):
+    """The `config` object of a bench line: the same keys in both arms (the
+    GPU search and the reference's CPU path), so the two lines describe one
+    workload."""
+    return {"workload": name, "grid": list(shape), "voxelspacing": cfg["voxelspacing"], "laplace": cfg["laplace"],
+            "core_weighted": cfg["core_weighted"], "rotation_set_size": int(nset),
+            "rotations_per_step": int(per_step), "l2": l2}
+
+
 # ---------------------------------------------------------------------------
 # clocks sampled during the timed region
 # ---------------------------------------------------------------------------
@@ -224,10 +233,8 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(r["wall_s"] for r in runs) / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded map, template, mask; %s)" % desc,
-        "config": {"workload": args.config, "grid": list(target.shape), "voxelspacing": cfg["voxelspacing"],
-                   "laplace": cfg["laplace"], "core_weighted": cfg["core_weighted"],
-                   "rotation_set_size": int(rot.shape[0]), "rotations_per_step": cores * per_core,
-                   "l2": "not applicable (host cores)"},
+        "config": workload_config(args.config, cfg, target.shape, int(rot.shape[0]), cores * per_core,
+                                  "not applicable (host cores)"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": "%d rotations per step (%d per core) from %s, _cpu_scan structure, numpy.fft; "
                                    "rate over the rotation loops (the per-process set-up, once per process in a "
@@ -469,10 +476,8 @@ def run_ours(args, rank, world, local_rank):
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 FFT / float-float LCC",
         "data": "synthetic (seeded map, template, mask; %s)" % desc,
-        "config": {"workload": args.config, "grid": list(shape), "voxelspacing": cfg["voxelspacing"],
-                   "laplace": cfg["laplace"], "core_weighted": cfg["core_weighted"],
-                   "rotation_set_size": nset, "rotations_per_step": per_step,
-                   "l2": "flushed (256 MiB write) before every timed step"},
+        "config": workload_config(args.config, cfg, shape, nset, per_step,
+                                  "flushed (256 MiB write) before every timed step"),
         # the search's own shapes (the reference arm has none): batch and
         # tiles from the autotuner, and the pruning geometry of this template
         "search": {"pairs_per_batch": pairs, "rows_pass1": ty1, "rows_pass3": ty3, "tuning": tuned,
