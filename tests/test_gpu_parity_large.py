@@ -9,7 +9,9 @@ the oracle restatement of ``CPUCorrelator.scan`` (``powerfitter.py:317-393``):
   ``make_golden.py`` from ``c48u2947.npy``);
 * 192^3, the precision-study workload (1.2 A/voxel, 8 copies of a 10,000-atom
   chain at 4.5 A, SNR 2), through the four-block clustered plane pass;
-* 160^3 and 96^3, maps of the uneven queue's sizes (one block a plane).
+* 160^3 and 96^3, maps of the uneven queue's sizes (one block a plane);
+* 105x84x90 and 128x96x80, non-cubic grids of the runtime-planned kernels
+  (radices 7, 5, 3 and a 2-3-smooth box).
 
 Criterion (as every parity test here): best LCC within 1e-4 absolute; best
 rotation identical wherever the oracle's top-two gap exceeds 1e-4.  The oracle
@@ -86,3 +88,17 @@ def test_scan_oracle_queue_sizes(n, vs, natoms, laplace):
     mask = determine_core_indices(c.mask) if laplace else c.mask
     rot = quat_to_rotmat(super_fibonacci(7416))[::1854]       # 4 rotations of the 9.72 degree set's size
     _parity(c.target.astype(np.float64), c.template, mask, rot, laplace, "%d^3" % n)
+
+
+@pytest.mark.parametrize("shape", [(105, 84, 90), (128, 96, 80)])
+def test_scan_oracle_large_non_cubic_runtime_planned(shape):
+    """Large non-cubic grids take the runtime-planned kernels: edges with the
+    radices 7, 5 and 3 (105 = 3*5*7, 84 = 2^2*3*7, 90 = 2*3^2*5) and a
+    2-3-smooth box, Laplace + core-weighted, against the oracle."""
+    from powerfit_gb300 import synth
+    from powerfit_gb300.correlator import determine_core_indices
+    from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
+    c = synth.make_case(shape, 2.0, 1500, 2, 7.0, 4.0, 60 + shape[0])
+    mask = determine_core_indices(c.mask)
+    rot = quat_to_rotmat(super_fibonacci(7416))[::1854]       # 4 rotations of the 9.72 degree set's size
+    _parity(c.target.astype(np.float64), c.template, mask, rot, True, "%dx%dx%d" % shape)
