@@ -622,8 +622,22 @@ __device__ __forceinline__ float lcc_value(float gcc, float ave, float ave2, flo
   return gcc * rsqrtf(var);
 }
 
+// The same in float64: the local variance Nm*ave2 - ave^2 and the division by
+// its square root.  The result is a float, so 1/sqrt(var) is taken to well
+// past float precision without float64 sqrt and divide: a float rsqrtf seed
+// (relative error ~2^-23) and one Newton-Raphson step for 1/sqrt in float64,
+// y1 = y0 (1 + (1 - var y0^2) / 2), whose relative error is about
+// 1.5 (2^-23)^2 ~ 2^-45; gcc * y1 is then rounded to float once.  Variances
+// outside the seed's normal float range, zero, negative or NaN take
+// gcc / sqrt(var) in float64 (its IEEE cases: +-inf, NaN).
 __device__ __forceinline__ float lcc_value64(float gcc, float ave, float ave2, float nm) {
   const double var = (double)ave2 * (double)nm - (double)ave * (double)ave;
+  if (var > 1e-30 && var < 1e30) {
+    const double y0 = (double)rsqrtf((float)var);
+    const double r = fma(-var * y0, y0, 1.0);
+    const double y1 = fma(0.5 * y0, r, y0);
+    return (float)((double)gcc * y1);
+  }
   return (float)((double)gcc / sqrt(var));
 }
 
