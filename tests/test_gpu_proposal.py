@@ -109,10 +109,11 @@ def test_proposal_full_fraction_equals_exhaustive(torch):
 
 
 def test_trained_network_ranks_best_fits_higher_than_coarse_score(torch):
-    """What the trained network gains over the method without it: on the
-    validation maps (96^3, the 207,576-rotation set) it ranks the exhaustive
-    best fit higher than the coarse score alone does, and always inside the
-    top 5% that the proposal re-searches."""
+    """What the trained network gains over the method without it: on eight
+    seeded 96^3 maps of the validation seeds (the 207,576-rotation set) it
+    ranks the exhaustive best fit higher than the coarse score alone does,
+    and always inside the top 5% of the set (TOP_FRACTION, the default
+    fraction of a proposal without a trained operating point)."""
     import math
     from powerfit_gb300 import proposal as PR, proposal_train as T
     from powerfit_gb300.rotations import quat_to_rotmat, super_fibonacci
